@@ -1,0 +1,213 @@
+/*
+ * mumfim_gpu.h -- C ABI of the GB300 batched explicit fiber-network RVE solver.
+ *
+ * This is the drop-in boundary for MuMFiM's batched microscale analysis. Every
+ * entry point below names the reference interface it replaces (paths are
+ * relative to the mumfim source tree).
+ *
+ * Conventions
+ *  - Plain C types only: host pointers + sizes in, integer status codes out.
+ *    No function calls exit() or abort(); failures return an mfg_status and
+ *    leave a message readable with mfg_last_error() (thread local).
+ *  - Deformation gradients are row-major 3x3 (F[r*9 + 3*i + j] = F_ij), the
+ *    same order the reference's DualView<Scalar*[3][3]> holds on the host.
+ *  - Stress is Cauchy stress in Voigt order [xx, yy, zz, yz, xz, xy]
+ *    (src/mumfim/microscale/batched_analysis/BatchedFiberRVEAnalysisExplicitBase.h:102-116).
+ *  - Material stiffness C[r*36 + 6*j + i] = d sigma_j / d (perturbation i),
+ *    i.e. C(rve, row j, column i) as in BatchedFiberRVEAnalysisExplicit.h:449-457.
+ *  - Node-indexed outputs are always in the caller's ORIGINAL node order; the
+ *    boundary-last reordering the solver uses internally is never visible.
+ *  - One mfg_batch must be used by one host thread at a time.
+ */
+#ifndef MUMFIM_GPU_H
+#define MUMFIM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MFG_ABI_VERSION 1
+
+/* Step cap applied in MFG_MODE_RELAX when mfg_strategy.max_steps <= 0. The
+ * reference loops without a cap (TeamOuterLoop.h:340-371); a cap turns a
+ * network that never relaxes into MFG_E_NOT_CONVERGED instead of a hang. */
+#define MFG_DEFAULT_STEP_CAP 1000000
+
+/* Status codes. The reference prints to cerr and calls std::exit on bad sizes
+ * (BatchedFiberRVEAnalysisExplicitBase.h:136-142,
+ * BatchedFiberRVEAnalysisExplicit.h:85-90,324-330) and reports nothing on
+ * non-convergence; these codes replace both behaviours. */
+typedef enum mfg_status {
+  MFG_OK = 0,
+  MFG_E_INVALID = 1,       /* bad argument, size mismatch, malformed network */
+  MFG_E_OOM = 2,           /* device or host allocation failed */
+  MFG_E_NOT_CONVERGED = 3, /* step cap reached before residual <= tol */
+  MFG_E_NONFINITE = 4,     /* NaN/Inf met in the residual or the stress */
+  MFG_E_TIMEOUT = 5,       /* a bounded wait gave up (serving queue) */
+  MFG_E_CUDA = 6,          /* a CUDA runtime call failed */
+  MFG_E_NO_DEVICE = 7,     /* no usable sm_103 device */
+  MFG_E_BUSY = 8           /* serving: no free slot / HBM for admission */
+} mfg_status;
+
+/* Fiber constitutive law ids, as in the .params format and the enum order of
+ * src/mumfim/microscale/FiberReactions.h:9-13 (linear = 0, nonlinear = 1). */
+typedef enum mfg_law { MFG_LAW_LINEAR = 0, MFG_LAW_NONLINEAR = 1 } mfg_law;
+
+/* One fiber reaction (FiberReactions.h:15-43). The fiber area is
+ * radius * radius * pi exactly as the .params reader forms it
+ * (FiberNetworkIO_impl.h:23-27). `B` and `length_ratio_trns` are used by the
+ * nonlinear law only; its compressive transition ratio is fixed at 1.0
+ * (FiberNetworkIO_impl.h:35). */
+typedef struct mfg_reaction {
+  int32_t law;
+  int32_t pad_;
+  double radius;
+  double youngs_modulus;
+  double density;
+  double B;
+  double length_ratio_trns;
+} mfg_reaction;
+
+/* One RVE's fiber network in the reference frame: the data the reference pulls
+ * out of the APF mesh in BatchedMesh.h:23-150. Nodes inside 1e-8 of a face of
+ * the cube [-0.5,0.5]^3 are the fixed boundary (RVE.h:86-103). As in the
+ * reference, only reaction 0 drives the batched solve
+ * (BatchedFiberRVEAnalysisExplicit.h:202-212). */
+typedef struct mfg_network {
+  int32_t n_nodes;
+  int32_t n_fibers;
+  const double* coords;        /* n_nodes x 3, row-major */
+  const int32_t* connectivity; /* n_fibers x 2, 0-based node ids */
+  mfg_reaction reaction;
+  double scale_factor; /* FiberNetwork::getScaleConversion(), default 1 */
+} mfg_network;
+
+/* Solve mode. RELAX is the reference's algorithm: affine predictor on every
+ * node, then damped explicit relaxation until the free-node residual is
+ * <= residual_tol, checked every 100 steps
+ * (BatchedFiberRVEAnalysisExplicitTeamOuterLoop.h:291-372). RAMP is the
+ * fixed-step protocol: no predictor, the boundary moves linearly from its
+ * start position to F * start over exactly max_steps steps. Both share the
+ * same step. */
+typedef enum mfg_mode { MFG_MODE_RELAX = 0, MFG_MODE_RAMP = 1 } mfg_mode;
+
+/* Per-RVE solution strategy (MicroSolutionStrategyExplicit, MicroFOParams.h:82-95).
+ * The reference's batched kernel ignores the configured critical time-scale
+ * factor and uses 0.8 (TeamOuterLoop.h:312); pass 0.8 for reference behaviour. */
+typedef struct mfg_strategy {
+  double visc_damp_coeff;        /* mass-proportional damping c */
+  double crit_time_scale_factor; /* dt = factor * l_min / sqrt(E/rho) */
+  double residual_tol;           /* reference: 1e-6 */
+  int32_t max_steps;             /* RELAX: step cap (<= 0: MFG_DEFAULT_STEP_CAP); RAMP: steps */
+  int32_t mode;                  /* mfg_mode */
+} mfg_strategy;
+
+/* Arithmetic of the solve. F64 is the plain kernel: IEEE FP64 with the
+ * reference's operation order and no contraction, bit-identical to a serial
+ * CPU run of the same algorithm. MIXED runs fiber forces and the integrator in
+ * FP32 on top of FP64 reference coordinates plus Kahan-compensated FP32
+ * displacements, and keeps FP64 for the stress, the residual and dt. */
+typedef enum mfg_precision { MFG_PREC_F64 = 0, MFG_PREC_MIXED = 1 } mfg_precision;
+
+typedef struct mfg_options {
+  int32_t precision;       /* mfg_precision */
+  int32_t device;          /* CUDA device ordinal */
+  int32_t threads_per_rve; /* CTA size; 0 = library default */
+  int32_t reserved[5];
+} mfg_options;
+
+/* Per-RVE outcome of one solve. */
+typedef struct mfg_rve_status {
+  int32_t status;  /* MFG_OK, MFG_E_NOT_CONVERGED or MFG_E_NONFINITE */
+  int32_t steps;   /* explicit steps taken */
+  double residual; /* last residual norm evaluated */
+} mfg_rve_status;
+
+typedef struct mfg_batch mfg_batch;
+
+/* ---- library ---------------------------------------------------------- */
+int32_t mfg_abi_version(void);
+const char* mfg_status_string(mfg_status s);
+/* Message of the last failure on the calling thread ("" when none). */
+const char* mfg_last_error(void);
+void mfg_default_strategy(mfg_strategy* out);
+void mfg_default_options(mfg_options* out);
+
+/* ---- batch lifecycle -------------------------------------------------- */
+/* Replaces BatchedFiberRVEAnalysisExplicit(fiber_networks, solution_strategies)
+ * (src/mumfim/microscale/BatchedFiberRVEAnalysisExplicit.h:80-256): finds the
+ * boundary, lumps the nodal mass (row-sum, rho*A*L0/2 per fiber end), builds
+ * the boundary-last permutation and the CSR fiber incidence, and uploads the
+ * batch to the device. `nets` and `strategies` hold n_rve entries each. */
+mfg_status mfg_batch_create(const mfg_network* nets, const mfg_strategy* strategies,
+                            int32_t n_rve, const mfg_options* options, mfg_batch** out);
+/* Frees every device and host resource of the batch. NULL is a no-op. */
+mfg_status mfg_batch_destroy(mfg_batch* batch);
+int32_t mfg_batch_size(const mfg_batch* batch);
+int32_t mfg_batch_n_nodes(const mfg_batch* batch, int32_t rve);
+int32_t mfg_batch_n_fibers(const mfg_batch* batch, int32_t rve);
+
+/* ---- the hot path ----------------------------------------------------- */
+/* Replaces BatchedRVEAnalysis::run(F, sigma, update_coords)
+ * (src/mumfim/microscale/BatchedRVEAnalysis.h:29-31; implementation
+ * BatchedFiberRVEAnalysisExplicit.h:257-320). F holds n_F row-major 3x3
+ * incremental deformation gradients; n_F == 1 broadcasts to every RVE
+ * (BatchedFiberRVEAnalysisExplicitBase.h:36) and is only valid with
+ * update_coords == 0, as in the reference. sigma receives n_rve x 6 Voigt
+ * Cauchy stresses. update_coords == 0 restores the displacement afterwards
+ * (the reference's transactional run). status (n_rve entries) may be NULL.
+ * Returns MFG_OK, or the worst per-RVE status, or an error. Blocking. */
+mfg_status mfg_batch_run(mfg_batch* batch, const double* F, int32_t n_F, double* sigma,
+                         int32_t update_coords, mfg_rve_status* status);
+/* Same solve with device-resident F (n_F x 9) and sigma (n_rve x 6) pointers,
+ * enqueued on `stream` (a cudaStream_t; NULL = the batch's own stream).
+ * Returns after enqueueing; status_dev (device, n_rve entries) may be NULL. */
+mfg_status mfg_batch_run_device(mfg_batch* batch, const double* F_dev, int32_t n_F,
+                                double* sigma_dev, int32_t update_coords,
+                                mfg_rve_status* status_dev, void* stream);
+/* Replaces BatchedRVEAnalysis::computeMaterialStiffness(C)
+ * (BatchedRVEAnalysis.h:36-37; BatchedFiberRVEAnalysisExplicit.h:321-405):
+ * six perturbed, non-updating solves at h = 1e-5 around the stress of the last
+ * updating run. C receives n_rve x 36 values, C[r*36 + 6*j + i]. */
+mfg_status mfg_batch_material_stiffness(mfg_batch* batch, double* C);
+/* Replaces compute3DOrientationTensor(omega) (BatchedRVEAnalysis.h:38-43;
+ * BatchedComputeOrientationTensor.h:145-186): mean n (x) n over fibers in the
+ * current configuration. omega: n_rve x 9, row-major. */
+mfg_status mfg_batch_orientation_3d(mfg_batch* batch, double* omega);
+/* Replaces compute2DOrientationTensor(normal, omega) (BatchedRVEAnalysis.h:44-50;
+ * BatchedComputeOrientationTensor.h:55-144): fiber directions projected onto
+ * the plane with the given normal (n_rve x 3) before averaging. */
+mfg_status mfg_batch_orientation_2d(mfg_batch* batch, const double* normal, double* omega);
+
+/* ---- state access ----------------------------------------------------- */
+/* Node displacement u = x - X of one RVE (n_nodes x 3, original order). */
+mfg_status mfg_batch_get_displacements(mfg_batch* batch, int32_t rve, double* u);
+/* Current coordinates x of one RVE (n_nodes x 3, original order). */
+mfg_status mfg_batch_get_coordinates(mfg_batch* batch, int32_t rve, double* x);
+/* Stress of the last updating run (the reference's current_stress_),
+ * n_rve x 6. */
+mfg_status mfg_batch_get_current_stress(mfg_batch* batch, double* sigma);
+/* Size in bytes of one RVE's exported state. */
+size_t mfg_batch_state_bytes(const mfg_batch* batch, int32_t rve);
+/* Copy one RVE's persistent state (u, x, volume, last stress) to / from a host
+ * buffer of mfg_batch_state_bytes() bytes. The reference keeps this state only
+ * in device memory between runs; export/import lets a caller evict and
+ * restore an RVE. */
+mfg_status mfg_batch_export_state(mfg_batch* batch, int32_t rve, void* buf, size_t bytes);
+mfg_status mfg_batch_import_state(mfg_batch* batch, int32_t rve, const void* buf, size_t bytes);
+
+/* ---- timing ----------------------------------------------------------- */
+/* Device time of the last run's relaxation kernel and of the whole run, in
+ * milliseconds, from CUDA events recorded on the launching stream. Valid
+ * after the run has completed on the device. */
+mfg_status mfg_batch_last_timing(mfg_batch* batch, float* relax_ms, float* run_ms);
+/* Number of kernels the last run launched. */
+int32_t mfg_batch_last_launches(const mfg_batch* batch);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MUMFIM_GPU_H */

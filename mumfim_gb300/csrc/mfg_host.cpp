@@ -1,0 +1,764 @@
+// Host side of the C ABI in include/mumfim_gpu.h.
+//
+// Set-up restates the constructor of the reference's batched analysis
+// (src/mumfim/microscale/BatchedFiberRVEAnalysisExplicit.h:80-256) on plain
+// arrays: boundary nodes (RVE.h:86-103, RVE_impl.h:5-20), row-sum lumped mass
+// (MassIntegrator.cc:16-56 via BatchedMesh.h:113-130), boundary-last
+// permutation (BatchedReorderMesh.h:54-73), plus the CSR fiber incidence the
+// GPU kernels gather forces over. Compiled with -ffp-contract=off: the mass
+// and reference lengths computed here feed the bit-exact FP64 kernel.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "mfg_internal.h"
+#include "mfg_mixed.h"
+#include "mumfim_gpu.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+mfg_status fail(mfg_status s, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return s;
+}
+
+#define MFG_CUDA(call)                                                                   \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(e_ == cudaErrorMemoryAllocation ? MFG_E_OOM : MFG_E_CUDA, "%s: %s (%s:%d)", \
+                  #call, cudaGetErrorString(e_), __FILE__, __LINE__);                    \
+  } while (0)
+
+// RVE(0.5).onBoundary(crd, side::all) with eps = 1e-8 (RVE.h:86-103).
+inline bool on_boundary(const double* crd) {
+  const double cr = 0.5, eps = 1e-8;
+  return std::fabs(cr * 1.0 - crd[0]) < eps || std::fabs(cr * -1.0 - crd[0]) < eps ||
+         std::fabs(cr * -1.0 - crd[1]) < eps || std::fabs(cr * 1.0 - crd[1]) < eps ||
+         std::fabs(cr * -1.0 - crd[2]) < eps || std::fabs(cr * 1.0 - crd[2]) < eps;
+}
+
+// getElementLength (BatchedFiberRVEAnalysisExplicitBase.h:203-215).
+inline double seg_length(const double* a, const double* b) {
+  double x1 = b[0] - a[0];
+  double x2 = b[1] - a[1];
+  double x3 = b[2] - a[2];
+  return std::sqrt(x1 * x1 + x2 * x2 + x3 * x3);
+}
+
+// Host-side product of the set-up of one RVE, solver (boundary-last) order.
+struct RveSetup {
+  int n_nodes = 0, n_free = 0, n_fibers = 0;
+  std::vector<int32_t> perm;  // original id -> solver id
+  std::vector<double> X;      // 3 x n_nodes, component blocks
+  std::vector<double> m;
+  std::vector<int32_t> conn;  // 2 x n_fibers interleaved (n1, n2)
+  std::vector<double> l0;
+  std::vector<int32_t> rowptr;  // n_nodes + 1
+  std::vector<int32_t> inc;     // 2 * n_fibers
+  std::string error;
+};
+
+void setup_rve(const mfg_network& net, RveSetup& s) {
+  const int N = net.n_nodes, E = net.n_fibers;
+  if (N < 2 || E < 1 || !net.coords || !net.connectivity) {
+    s.error = "network needs at least 2 nodes, 1 fiber and non-null arrays";
+    return;
+  }
+  for (int64_t k = 0; k < 3LL * N; ++k)
+    if (!std::isfinite(net.coords[k])) {
+      s.error = "non-finite node coordinate";
+      return;
+    }
+  for (int e = 0; e < E; ++e) {
+    int a = net.connectivity[2 * e], b = net.connectivity[2 * e + 1];
+    if (a < 0 || b < 0 || a >= N || b >= N) {
+      s.error = "fiber " + std::to_string(e) + " references a node outside [0, n_nodes)";
+      return;
+    }
+    if (a == b) {
+      s.error = "fiber " + std::to_string(e) + " is a self-loop";
+      return;
+    }
+  }
+  const mfg_reaction& rc = net.reaction;
+  const double area = rc.radius * rc.radius * M_PI;  // FiberNetworkIO_impl.h:26
+  // boundary list in mesh order (BatchedFiberRVEAnalysisExplicit.h:190-202)
+  std::vector<int32_t> fixed;
+  for (int i = 0; i < N; ++i)
+    if (on_boundary(&net.coords[3 * i])) fixed.push_back(i);
+  const int nb = static_cast<int>(fixed.size());
+  // row-sum lumped mass, original order, fiber order
+  std::vector<double> mass(N, 0.0);
+  std::vector<int> degree(N, 0);
+  for (int e = 0; e < E; ++e) {
+    int n1 = net.connectivity[2 * e], n2 = net.connectivity[2 * e + 1];
+    double l0 = seg_length(&net.coords[3 * n1], &net.coords[3 * n2]);
+    if (!(l0 > 0.0)) {
+      s.error = "fiber " + std::to_string(e) + " has zero length";
+      return;
+    }
+    double me = rc.density * area * l0 * 0.5;
+    mass[n1] = mass[n1] + me;
+    mass[n2] = mass[n2] + me;
+    degree[n1]++;
+    degree[n2]++;
+  }
+  // boundary-last permutation (BatchedReorderMesh.h:54-73)
+  s.perm.assign(N, 0);
+  for (int i = 0; i < nb; ++i) s.perm[fixed[i]] = i + 1;
+  int update = 0;
+  for (int i = 0; i < N; ++i) {
+    int val = s.perm[i];
+    bool is_fixed = val > 0;
+    update += is_fixed ? 1 : 0;
+    s.perm[i] = is_fixed ? (N - nb) + (val - 1) : i - update;
+  }
+  for (int i = 0; i < N; ++i)
+    if (degree[i] == 0 && s.perm[i] < N - nb) {
+      s.error = "free node " + std::to_string(i) + " has no fibers (zero lumped mass)";
+      return;
+    }
+  s.n_nodes = N;
+  s.n_free = N - nb;
+  s.n_fibers = E;
+  s.X.assign(3 * static_cast<size_t>(N), 0.0);
+  s.m.assign(N, 0.0);
+  for (int i = 0; i < N; ++i) {
+    int p = s.perm[i];
+    for (int k = 0; k < 3; ++k) s.X[static_cast<size_t>(k) * N + p] = net.coords[3 * i + k];
+    s.m[p] = mass[i];
+  }
+  s.conn.resize(2 * static_cast<size_t>(E));
+  s.l0.resize(E);
+  std::vector<int32_t> cnt(N + 1, 0);
+  for (int e = 0; e < E; ++e) {
+    int a = s.perm[net.connectivity[2 * e]], b = s.perm[net.connectivity[2 * e + 1]];
+    s.conn[2 * e] = a;
+    s.conn[2 * e + 1] = b;
+    double pa[3] = {s.X[a], s.X[N + a], s.X[2 * static_cast<size_t>(N) + a]};
+    double pb[3] = {s.X[b], s.X[N + b], s.X[2 * static_cast<size_t>(N) + b]};
+    s.l0[e] = seg_length(pa, pb);
+    cnt[a + 1]++;
+    cnt[b + 1]++;
+  }
+  // CSR incidence: fibers in ascending id per node; end 0 = first node.
+  s.rowptr.assign(N + 1, 0);
+  for (int i = 0; i < N; ++i) s.rowptr[i + 1] = s.rowptr[i] + cnt[i + 1];
+  s.inc.resize(2 * static_cast<size_t>(E));
+  std::vector<int32_t> fill(s.rowptr.begin(), s.rowptr.end() - 1);
+  for (int e = 0; e < E; ++e)
+    for (int j = 0; j < 2; ++j) s.inc[fill[s.conn[2 * e + j]]++] = (e << 1) | j;
+}
+
+template <typename Fn>
+void parallel_for(int n, Fn fn) {
+  int nt = static_cast<int>(std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), 32u));
+  if (n < 4 || nt <= 1) {
+    for (int i = 0; i < n; ++i) fn(i);
+    return;
+  }
+  nt = std::min(nt, n);
+  std::atomic<int> next{0};
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; ++t)
+    th.emplace_back([&]() {
+      for (int i = next++; i < n; i = next++) fn(i);
+    });
+  for (auto& x : th) x.join();
+}
+
+template <typename T>
+struct DevArray {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t alloc(size_t count) {
+    n = std::max<size_t>(count, 1);
+    return cudaMalloc(&p, n * sizeof(T));
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+  }
+};
+
+}  // namespace
+
+struct mfg_batch {
+  int device = 0;
+  int precision = MFG_PREC_F64;
+  int R = 0;
+  int64_t nt = 0, et = 0, nbt = 0;
+  std::vector<int> n_nodes, n_free, n_fibers;
+  std::vector<std::vector<int32_t>> perm;
+  std::vector<mfg::RveDesc> desc;
+  int sms = 1;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev_run0 = nullptr, ev_relax0 = nullptr, ev_relax1 = nullptr, ev_run1 = nullptr;
+  int last_launches = 0;
+  bool timing_valid = false;
+  // device buffers
+  DevArray<mfg::RveDesc> d_desc;
+  DevArray<double> d_X, d_x, d_u, d_v, d_m, d_l0, d_nrm, d_fint, d_ramp, d_vol, d_cur;
+  DevArray<int2> d_conn;
+  DevArray<int32_t> d_rowptr, d_inc, d_order, d_queue;
+  // per-run scratch
+  DevArray<double> d_F, d_sigma, d_res, d_omega;
+  DevArray<int32_t> d_status, d_steps;
+  DevArray<mfg_rve_status> d_st;
+  mfg::DevBatch dev{};
+  std::unique_ptr<mfg::MixedState, mfg::MixedStateDeleter> mixed;
+
+  ~mfg_batch() {
+    if (device >= 0) cudaSetDevice(device);
+    mixed.reset();
+    for (auto* a : {&d_X, &d_x, &d_u, &d_v, &d_m, &d_l0, &d_nrm, &d_fint, &d_ramp, &d_vol, &d_cur,
+                    &d_F, &d_sigma, &d_res, &d_omega})
+      a->release();
+    d_desc.release();
+    d_conn.release();
+    for (auto* a : {&d_rowptr, &d_inc, &d_order, &d_queue, &d_status, &d_steps}) a->release();
+    d_st.release();
+    for (auto* e : {&ev_run0, &ev_relax0, &ev_relax1, &ev_run1})
+      if (*e) cudaEventDestroy(*e);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+mfg_status check_strategy(const mfg_strategy& s, int r) {
+  if (!(s.visc_damp_coeff >= 0.0) || !std::isfinite(s.visc_damp_coeff))
+    return fail(MFG_E_INVALID, "rve %d: damping must be finite and >= 0", r);
+  if (!(s.crit_time_scale_factor > 0.0) || !std::isfinite(s.crit_time_scale_factor))
+    return fail(MFG_E_INVALID, "rve %d: critical time scale factor must be > 0", r);
+  if (!(s.residual_tol >= 0.0) || !std::isfinite(s.residual_tol))
+    return fail(MFG_E_INVALID, "rve %d: residual tolerance must be finite and >= 0", r);
+  if (s.mode != MFG_MODE_RELAX && s.mode != MFG_MODE_RAMP)
+    return fail(MFG_E_INVALID, "rve %d: unknown mode %d", r, s.mode);
+  if (s.mode == MFG_MODE_RAMP && s.max_steps < 1)
+    return fail(MFG_E_INVALID, "rve %d: RAMP mode needs max_steps >= 1", r);
+  return MFG_OK;
+}
+
+mfg_status check_reaction(const mfg_reaction& rc, int r) {
+  if (rc.law != MFG_LAW_LINEAR && rc.law != MFG_LAW_NONLINEAR)
+    return fail(MFG_E_INVALID, "rve %d: unknown fiber law %d", r, rc.law);
+  if (!(rc.radius > 0) || !(rc.youngs_modulus > 0) || !(rc.density > 0) ||
+      !std::isfinite(rc.radius) || !std::isfinite(rc.youngs_modulus) || !std::isfinite(rc.density))
+    return fail(MFG_E_INVALID, "rve %d: radius, modulus and density must be finite and > 0", r);
+  if (rc.law == MFG_LAW_NONLINEAR &&
+      (!(rc.B > 0) || !std::isfinite(rc.B) || !(rc.length_ratio_trns >= 1.0) ||
+       !std::isfinite(rc.length_ratio_trns)))
+    return fail(MFG_E_INVALID, "rve %d: nonlinear law needs B > 0 and length_ratio_trns >= 1", r);
+  return MFG_OK;
+}
+
+template <typename T>
+mfg_status upload(DevArray<T>& d, const std::vector<T>& h, cudaStream_t s) {
+  MFG_CUDA(d.alloc(h.size()));
+  if (!h.empty()) MFG_CUDA(cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  return MFG_OK;
+}
+
+mfg_status enqueue_run(mfg_batch* b, const double* F_dev, int32_t n_F, double* sigma_dev,
+                       int32_t update_coords, cudaStream_t s) {
+  MFG_CUDA(cudaMemsetAsync(b->d_queue.p, 0, sizeof(int32_t), s));
+  mfg::RunArgs a{};
+  a.F = F_dev;
+  a.n_F = n_F;
+  a.update_coords = update_coords;
+  a.sigma = sigma_dev;
+  a.st_status = b->d_status.p;
+  a.st_steps = b->d_steps.p;
+  a.st_residual = b->d_res.p;
+  MFG_CUDA(cudaEventRecord(b->ev_relax0, s));
+  cudaError_t e;
+  if (b->precision == MFG_PREC_MIXED) {
+    e = mfg::run_mixed(*b->mixed, b->dev, a, s, &b->last_launches);
+  } else {
+    int occ = mfg::relax_f64_max_blocks_per_sm(0);
+    int grid = std::min(b->R, b->sms * occ);
+    e = mfg::launch_relax_f64(b->dev, a, 0, grid, s);
+    b->last_launches = 1;
+  }
+  if (e != cudaSuccess)
+    return fail(MFG_E_CUDA, "relaxation launch failed: %s", cudaGetErrorString(e));
+  MFG_CUDA(cudaEventRecord(b->ev_relax1, s));
+  return MFG_OK;
+}
+
+mfg_status check_run_args(mfg_batch* b, int32_t n_F, int32_t update_coords) {
+  if (n_F != 1 && n_F != b->R)
+    return fail(MFG_E_INVALID, "F must hold 1 or n_rve (%d) matrices, got %d", b->R, n_F);
+  if (update_coords && n_F != b->R)
+    // BatchedFiberRVEAnalysisExplicitBase.h:136-142
+    return fail(MFG_E_INVALID,
+                "The volume and deformation gradients must have the same extent corresponding "
+                "to the number of RVEs.");
+  return MFG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t mfg_abi_version(void) { return MFG_ABI_VERSION; }
+
+const char* mfg_status_string(mfg_status s) {
+  switch (s) {
+    case MFG_OK: return "MFG_OK";
+    case MFG_E_INVALID: return "MFG_E_INVALID";
+    case MFG_E_OOM: return "MFG_E_OOM";
+    case MFG_E_NOT_CONVERGED: return "MFG_E_NOT_CONVERGED";
+    case MFG_E_NONFINITE: return "MFG_E_NONFINITE";
+    case MFG_E_TIMEOUT: return "MFG_E_TIMEOUT";
+    case MFG_E_CUDA: return "MFG_E_CUDA";
+    case MFG_E_NO_DEVICE: return "MFG_E_NO_DEVICE";
+    case MFG_E_BUSY: return "MFG_E_BUSY";
+  }
+  return "MFG_E_UNKNOWN";
+}
+
+const char* mfg_last_error(void) { return g_last_error.c_str(); }
+
+void mfg_default_strategy(mfg_strategy* out) {
+  if (!out) return;
+  out->visc_damp_coeff = 0.5;
+  out->crit_time_scale_factor = 0.8;
+  out->residual_tol = 1e-6;
+  out->max_steps = 0;
+  out->mode = MFG_MODE_RELAX;
+}
+
+void mfg_default_options(mfg_options* out) {
+  if (!out) return;
+  std::memset(out, 0, sizeof(*out));
+  out->precision = MFG_PREC_F64;
+}
+
+mfg_status mfg_batch_create(const mfg_network* nets, const mfg_strategy* strategies,
+                            int32_t n_rve, const mfg_options* options, mfg_batch** out) {
+  g_last_error.clear();
+  if (!out) return fail(MFG_E_INVALID, "out is NULL");
+  *out = nullptr;
+  if (!nets || !strategies || n_rve < 1)
+    return fail(MFG_E_INVALID, "There must be a solution strategy for each fiber network!");
+  mfg_options opt;
+  mfg_default_options(&opt);
+  if (options) opt = *options;
+  if (opt.precision != MFG_PREC_F64 && opt.precision != MFG_PREC_MIXED)
+    return fail(MFG_E_INVALID, "unknown precision %d", opt.precision);
+  for (int r = 0; r < n_rve; ++r) {
+    mfg_status st = check_strategy(strategies[r], r);
+    if (st != MFG_OK) return st;
+    st = check_reaction(nets[r].reaction, r);
+    if (st != MFG_OK) return st;
+    if (!(nets[r].scale_factor > 0) || !std::isfinite(nets[r].scale_factor))
+      return fail(MFG_E_INVALID, "rve %d: scale factor must be finite and > 0", r);
+  }
+  // ---- host set-up, in parallel over RVEs ------------------------------
+  std::vector<RveSetup> su(n_rve);
+  parallel_for(n_rve, [&](int r) { setup_rve(nets[r], su[r]); });
+  for (int r = 0; r < n_rve; ++r)
+    if (!su[r].error.empty()) return fail(MFG_E_INVALID, "rve %d: %s", r, su[r].error.c_str());
+
+  // ---- device ------------------------------------------------------------
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
+    return fail(MFG_E_NO_DEVICE, "no CUDA device available");
+  if (opt.device < 0 || opt.device >= ndev)
+    return fail(MFG_E_NO_DEVICE, "device %d out of range (%d devices)", opt.device, ndev);
+  MFG_CUDA(cudaSetDevice(opt.device));
+  cudaDeviceProp prop;
+  MFG_CUDA(cudaGetDeviceProperties(&prop, opt.device));
+  if (prop.major < 10)
+    return fail(MFG_E_NO_DEVICE, "device %d (%s, sm_%d%d) is not a Blackwell GPU", opt.device,
+                prop.name, prop.major, prop.minor);
+
+  std::unique_ptr<mfg_batch> b(new mfg_batch());
+  b->device = opt.device;
+  b->precision = opt.precision;
+  b->R = n_rve;
+  b->sms = prop.multiProcessorCount;
+  b->n_nodes.resize(n_rve);
+  b->n_free.resize(n_rve);
+  b->n_fibers.resize(n_rve);
+  b->perm.resize(n_rve);
+  b->desc.resize(n_rve);
+  int64_t no = 0, fo = 0, io = 0, ro = 0, bo = 0;
+  for (int r = 0; r < n_rve; ++r) {
+    const RveSetup& s = su[r];
+    mfg::RveDesc& d = b->desc[r];
+    std::memset(&d, 0, sizeof(d));
+    d.node_off = no;
+    d.fiber_off = fo;
+    d.inc_off = io;
+    d.row_off = ro;
+    d.bnd_off = bo;
+    d.n_nodes = s.n_nodes;
+    d.n_free = s.n_free;
+    d.n_fibers = s.n_fibers;
+    const mfg_reaction& rc = nets[r].reaction;
+    const mfg_strategy& st = strategies[r];
+    d.law = rc.law;
+    d.E = rc.youngs_modulus;
+    d.A = rc.radius * rc.radius * M_PI;
+    d.B = rc.B;
+    d.lt = rc.length_ratio_trns;
+    d.c = st.visc_damp_coeff;
+    d.crit = st.crit_time_scale_factor;
+    d.tol = st.residual_tol;
+    d.mode = st.mode;
+    d.max_steps = st.mode == MFG_MODE_RAMP ? st.max_steps
+                                           : (st.max_steps > 0 ? st.max_steps : MFG_DEFAULT_STEP_CAP);
+    d.sound_speed = std::sqrt(rc.youngs_modulus / rc.density);  // TeamOuterLoop.h:72
+    d.scale = nets[r].scale_factor;
+    no += s.n_nodes;
+    fo += s.n_fibers;
+    io += 2LL * s.n_fibers;
+    ro += s.n_nodes + 1;
+    bo += s.n_nodes - s.n_free;
+    b->n_nodes[r] = s.n_nodes;
+    b->n_free[r] = s.n_free;
+    b->n_fibers[r] = s.n_fibers;
+    b->perm[r] = s.perm;
+  }
+  b->nt = no;
+  b->et = fo;
+  b->nbt = bo;
+  const int64_t nt = no, et = fo;
+
+  // ---- pack ------------------------------------------------------------
+  std::vector<double> X(3 * nt), m(nt), l0(et);
+  std::vector<int2> conn(et);
+  std::vector<int32_t> rowptr(ro), inc(io);
+  parallel_for(n_rve, [&](int r) {
+    const RveSetup& s = su[r];
+    const mfg::RveDesc& d = b->desc[r];
+    const int N = s.n_nodes;
+    for (int k = 0; k < 3; ++k)
+      std::memcpy(&X[k * nt + d.node_off], &s.X[static_cast<size_t>(k) * N], N * sizeof(double));
+    std::memcpy(&m[d.node_off], s.m.data(), N * sizeof(double));
+    for (int e = 0; e < s.n_fibers; ++e) conn[d.fiber_off + e] = make_int2(s.conn[2 * e], s.conn[2 * e + 1]);
+    std::memcpy(&l0[d.fiber_off], s.l0.data(), s.n_fibers * sizeof(double));
+    std::memcpy(&rowptr[d.row_off], s.rowptr.data(), (N + 1) * sizeof(int32_t));
+    std::memcpy(&inc[d.inc_off], s.inc.data(), 2 * s.n_fibers * sizeof(int32_t));
+  });
+  // persistent-queue order: most fibers first (longest-processing-time first)
+  std::vector<int32_t> order(n_rve);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+    return b->n_fibers[a] > b->n_fibers[c];
+  });
+
+  // ---- device ------------------------------------------------------------
+  MFG_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  for (auto* e : {&b->ev_run0, &b->ev_relax0, &b->ev_relax1, &b->ev_run1})
+    MFG_CUDA(cudaEventCreate(e));
+  cudaStream_t s = b->stream;
+  mfg_status st;
+  if ((st = upload(b->d_desc, b->desc, s)) != MFG_OK) return st;
+  if ((st = upload(b->d_X, X, s)) != MFG_OK) return st;
+  MFG_CUDA(b->d_x.alloc(3 * nt));
+  MFG_CUDA(cudaMemcpyAsync(b->d_x.p, b->d_X.p, 3 * nt * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  MFG_CUDA(b->d_u.alloc(3 * nt));
+  MFG_CUDA(cudaMemsetAsync(b->d_u.p, 0, 3 * nt * sizeof(double), s));
+  MFG_CUDA(b->d_v.alloc(3 * nt));
+  MFG_CUDA(cudaMemsetAsync(b->d_v.p, 0, 3 * nt * sizeof(double), s));
+  MFG_CUDA(b->d_fint.alloc(3 * nt));
+  MFG_CUDA(cudaMemsetAsync(b->d_fint.p, 0, 3 * nt * sizeof(double), s));
+  if ((st = upload(b->d_m, m, s)) != MFG_OK) return st;
+  if ((st = upload(b->d_conn, conn, s)) != MFG_OK) return st;
+  if ((st = upload(b->d_l0, l0, s)) != MFG_OK) return st;
+  MFG_CUDA(b->d_nrm.alloc(3 * et));
+  if ((st = upload(b->d_rowptr, rowptr, s)) != MFG_OK) return st;
+  if ((st = upload(b->d_inc, inc, s)) != MFG_OK) return st;
+  MFG_CUDA(b->d_ramp.alloc(6 * std::max<int64_t>(b->nbt, 1)));
+  std::vector<double> ones(n_rve, 1.0);  // BatchedFiberRVEAnalysisExplicit.h:115-118
+  if ((st = upload(b->d_vol, ones, s)) != MFG_OK) return st;
+  MFG_CUDA(b->d_cur.alloc(6 * n_rve));
+  MFG_CUDA(cudaMemsetAsync(b->d_cur.p, 0, 6 * n_rve * sizeof(double), s));
+  if ((st = upload(b->d_order, order, s)) != MFG_OK) return st;
+  MFG_CUDA(b->d_queue.alloc(1));
+  MFG_CUDA(b->d_F.alloc(9 * n_rve));
+  MFG_CUDA(b->d_sigma.alloc(6 * n_rve));
+  MFG_CUDA(b->d_omega.alloc(9 * n_rve));
+  MFG_CUDA(b->d_res.alloc(n_rve));
+  MFG_CUDA(b->d_status.alloc(n_rve));
+  MFG_CUDA(b->d_steps.alloc(n_rve));
+  MFG_CUDA(b->d_st.alloc(n_rve));
+
+  mfg::DevBatch& dv = b->dev;
+  dv.n_rve = n_rve;
+  dv.nt = nt;
+  dv.et = et;
+  dv.desc = b->d_desc.p;
+  dv.X = b->d_X.p;
+  dv.x = b->d_x.p;
+  dv.u = b->d_u.p;
+  dv.v = b->d_v.p;
+  dv.m = b->d_m.p;
+  dv.conn = b->d_conn.p;
+  dv.l0 = b->d_l0.p;
+  dv.nrm = b->d_nrm.p;
+  dv.fint = b->d_fint.p;
+  dv.rowptr = b->d_rowptr.p;
+  dv.inc = b->d_inc.p;
+  dv.ramp = b->d_ramp.p;
+  dv.vol = b->d_vol.p;
+  dv.cur_stress = b->d_cur.p;
+  dv.order = b->d_order.p;
+  dv.queue = b->d_queue.p;
+  if (b->precision == MFG_PREC_MIXED) {
+    b->mixed.reset(mfg::mixed_new());
+    cudaError_t e = b->mixed ? mfg::mixed_create(*b->mixed, dv, b->desc, b->sms, s)
+                             : cudaErrorMemoryAllocation;
+    if (e != cudaSuccess)
+      return fail(e == cudaErrorMemoryAllocation ? MFG_E_OOM : MFG_E_CUDA,
+                  "mixed-precision set-up failed: %s", cudaGetErrorString(e));
+  }
+  MFG_CUDA(cudaStreamSynchronize(s));
+  *out = b.release();
+  return MFG_OK;
+}
+
+mfg_status mfg_batch_destroy(mfg_batch* batch) {
+  delete batch;
+  return MFG_OK;
+}
+
+int32_t mfg_batch_size(const mfg_batch* b) { return b ? b->R : 0; }
+int32_t mfg_batch_n_nodes(const mfg_batch* b, int32_t r) {
+  return (b && r >= 0 && r < b->R) ? b->n_nodes[r] : -1;
+}
+int32_t mfg_batch_n_fibers(const mfg_batch* b, int32_t r) {
+  return (b && r >= 0 && r < b->R) ? b->n_fibers[r] : -1;
+}
+
+mfg_status mfg_batch_run_device(mfg_batch* b, const double* F_dev, int32_t n_F, double* sigma_dev,
+                                int32_t update_coords, mfg_rve_status* status_dev, void* stream) {
+  g_last_error.clear();
+  if (!b || !F_dev || !sigma_dev) return fail(MFG_E_INVALID, "NULL argument");
+  mfg_status st = check_run_args(b, n_F, update_coords);
+  if (st != MFG_OK) return st;
+  MFG_CUDA(cudaSetDevice(b->device));
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : b->stream;
+  b->timing_valid = false;
+  MFG_CUDA(cudaEventRecord(b->ev_run0, s));
+  if ((st = enqueue_run(b, F_dev, n_F, sigma_dev, update_coords, s)) != MFG_OK) return st;
+  if (status_dev) {
+    cudaError_t e = mfg::launch_pack_status(b->d_status.p, b->d_steps.p, b->d_res.p, b->R,
+                                            status_dev, s);
+    if (e != cudaSuccess) return fail(MFG_E_CUDA, "status pack failed: %s", cudaGetErrorString(e));
+    b->last_launches += 1;
+  }
+  MFG_CUDA(cudaEventRecord(b->ev_run1, s));
+  b->timing_valid = true;
+  return MFG_OK;
+}
+
+mfg_status mfg_batch_run(mfg_batch* b, const double* F, int32_t n_F, double* sigma,
+                         int32_t update_coords, mfg_rve_status* status) {
+  g_last_error.clear();
+  if (!b || !F || !sigma) return fail(MFG_E_INVALID, "NULL argument");
+  mfg_status st = check_run_args(b, n_F, update_coords);
+  if (st != MFG_OK) return st;
+  MFG_CUDA(cudaSetDevice(b->device));
+  cudaStream_t s = b->stream;
+  b->timing_valid = false;
+  MFG_CUDA(cudaEventRecord(b->ev_run0, s));
+  MFG_CUDA(cudaMemcpyAsync(b->d_F.p, F, 9 * sizeof(double) * n_F, cudaMemcpyHostToDevice, s));
+  if ((st = enqueue_run(b, b->d_F.p, n_F, b->d_sigma.p, update_coords, s)) != MFG_OK) return st;
+  cudaError_t e = mfg::launch_pack_status(b->d_status.p, b->d_steps.p, b->d_res.p, b->R,
+                                          b->d_st.p, s);
+  if (e != cudaSuccess) return fail(MFG_E_CUDA, "status pack failed: %s", cudaGetErrorString(e));
+  b->last_launches += 1;
+  std::vector<mfg_rve_status> hst(b->R);
+  MFG_CUDA(cudaMemcpyAsync(sigma, b->d_sigma.p, 6 * sizeof(double) * b->R, cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(cudaMemcpyAsync(hst.data(), b->d_st.p, sizeof(mfg_rve_status) * b->R,
+                           cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(cudaEventRecord(b->ev_run1, s));
+  MFG_CUDA(cudaStreamSynchronize(s));
+  b->timing_valid = true;
+  int worst = MFG_OK;
+  for (int r = 0; r < b->R; ++r) {
+    if (status) status[r] = hst[r];
+    if (hst[r].status > worst) worst = hst[r].status;
+  }
+  if (worst != MFG_OK)
+    fail(static_cast<mfg_status>(worst), "%s in at least one RVE",
+         mfg_status_string(static_cast<mfg_status>(worst)));
+  return static_cast<mfg_status>(worst);
+}
+
+mfg_status mfg_batch_material_stiffness(mfg_batch* b, double* C) {
+  g_last_error.clear();
+  if (!b || !C) return fail(MFG_E_INVALID, "NULL argument");
+  MFG_CUDA(cudaSetDevice(b->device));
+  // BatchedFiberRVEAnalysisExplicit.h:321-405
+  constexpr double h = 1E-5;
+  double D1 = std::sqrt(1.0 / (1 - 2 * h));
+  constexpr double l1 = 1;
+  constexpr double l2 = (1 + h) / (1 - h * h);
+  constexpr double l3 = (1 - h) / (1 - h * h);
+  double l2pl3 = 0.5 * (std::sqrt(l2) + std::sqrt(l3));
+  double l2ml3 = 0.5 * (std::sqrt(l2) - std::sqrt(l3));
+  std::vector<double> cur(6 * b->R), sigma1(6 * b->R);
+  MFG_CUDA(cudaMemcpy(cur.data(), b->d_cur.p, 6 * sizeof(double) * b->R, cudaMemcpyDeviceToHost));
+  mfg_status worst = MFG_OK;
+  for (int i = 0; i < 6; ++i) {
+    double Fa[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    switch (i) {
+      case 0: Fa[0] = D1; Fa[4] = 1; Fa[8] = 1; break;
+      case 1: Fa[0] = 1; Fa[4] = D1; Fa[8] = 1; break;
+      case 2: Fa[0] = 1; Fa[4] = 1; Fa[8] = D1; break;
+      case 3: Fa[0] = l1; Fa[4] = l2pl3; Fa[8] = l2pl3; Fa[5] = l2ml3; Fa[7] = l2ml3; break;
+      case 4: Fa[0] = l2pl3; Fa[4] = l1; Fa[8] = l2pl3; Fa[2] = l2ml3; Fa[6] = l2ml3; break;
+      default: Fa[0] = l2pl3; Fa[4] = l2pl3; Fa[8] = l1; Fa[1] = l2ml3; Fa[3] = l2ml3; break;
+    }
+    mfg_status st = mfg_batch_run(b, Fa, 1, sigma1.data(), 0, nullptr);
+    if (st == MFG_E_INVALID || st == MFG_E_CUDA || st == MFG_E_OOM) return st;
+    if (st > worst) worst = st;
+    for (int r = 0; r < b->R; ++r)
+      for (int j = 0; j < 6; ++j) C[36 * r + 6 * j + i] = (sigma1[6 * r + j] - cur[6 * r + j]) / h;
+  }
+  return worst;
+}
+
+mfg_status mfg_batch_orientation_3d(mfg_batch* b, double* omega) {
+  return mfg_batch_orientation_2d(b, nullptr, omega);
+}
+
+mfg_status mfg_batch_orientation_2d(mfg_batch* b, const double* normal, double* omega) {
+  g_last_error.clear();
+  if (!b || !omega) return fail(MFG_E_INVALID, "NULL argument");
+  MFG_CUDA(cudaSetDevice(b->device));
+  cudaStream_t s = b->stream;
+  const double* nd = nullptr;
+  if (normal) {
+    MFG_CUDA(cudaMemcpyAsync(b->d_F.p, normal, 3 * sizeof(double) * b->R, cudaMemcpyHostToDevice, s));
+    nd = b->d_F.p;
+  }
+  cudaError_t e = mfg::launch_orientation(b->dev, nd, b->d_omega.p, s);
+  if (e != cudaSuccess) return fail(MFG_E_CUDA, "orientation launch failed: %s", cudaGetErrorString(e));
+  MFG_CUDA(cudaMemcpyAsync(omega, b->d_omega.p, 9 * sizeof(double) * b->R, cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(cudaStreamSynchronize(s));
+  return MFG_OK;
+}
+
+static mfg_status get_node_field(mfg_batch* b, int32_t rve, const double* field, double* out) {
+  if (!b || !out || rve < 0 || rve >= b->R) return fail(MFG_E_INVALID, "bad rve or NULL output");
+  MFG_CUDA(cudaSetDevice(b->device));
+  const mfg::RveDesc& d = b->desc[rve];
+  const int N = d.n_nodes;
+  std::vector<double> tmp(3 * static_cast<size_t>(N));
+  for (int k = 0; k < 3; ++k)
+    MFG_CUDA(cudaMemcpyAsync(&tmp[static_cast<size_t>(k) * N], field + k * b->nt + d.node_off,
+                             N * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  MFG_CUDA(cudaStreamSynchronize(b->stream));
+  const auto& perm = b->perm[rve];
+  for (int i = 0; i < N; ++i)
+    for (int k = 0; k < 3; ++k) out[3 * i + k] = tmp[static_cast<size_t>(k) * N + perm[i]];
+  return MFG_OK;
+}
+
+mfg_status mfg_batch_get_displacements(mfg_batch* b, int32_t rve, double* u) {
+  g_last_error.clear();
+  return get_node_field(b, rve, b ? b->d_u.p : nullptr, u);
+}
+
+mfg_status mfg_batch_get_coordinates(mfg_batch* b, int32_t rve, double* x) {
+  g_last_error.clear();
+  return get_node_field(b, rve, b ? b->d_x.p : nullptr, x);
+}
+
+mfg_status mfg_batch_get_current_stress(mfg_batch* b, double* sigma) {
+  g_last_error.clear();
+  if (!b || !sigma) return fail(MFG_E_INVALID, "NULL argument");
+  MFG_CUDA(cudaSetDevice(b->device));
+  MFG_CUDA(cudaMemcpy(sigma, b->d_cur.p, 6 * sizeof(double) * b->R, cudaMemcpyDeviceToHost));
+  return MFG_OK;
+}
+
+size_t mfg_batch_state_bytes(const mfg_batch* b, int32_t rve) {
+  if (!b || rve < 0 || rve >= b->R) return 0;
+  return (6 * static_cast<size_t>(b->n_nodes[rve]) + 7) * sizeof(double);
+}
+
+mfg_status mfg_batch_export_state(mfg_batch* b, int32_t rve, void* buf, size_t bytes) {
+  g_last_error.clear();
+  if (!b || !buf || rve < 0 || rve >= b->R) return fail(MFG_E_INVALID, "bad rve or NULL buffer");
+  if (bytes < mfg_batch_state_bytes(b, rve)) return fail(MFG_E_INVALID, "buffer too small");
+  MFG_CUDA(cudaSetDevice(b->device));
+  const mfg::RveDesc& d = b->desc[rve];
+  const size_t N = d.n_nodes;
+  double* o = static_cast<double*>(buf);
+  for (int k = 0; k < 3; ++k) {
+    MFG_CUDA(cudaMemcpyAsync(o + k * N, b->d_u.p + k * b->nt + d.node_off, N * sizeof(double),
+                             cudaMemcpyDeviceToHost, b->stream));
+    MFG_CUDA(cudaMemcpyAsync(o + (3 + k) * N, b->d_x.p + k * b->nt + d.node_off, N * sizeof(double),
+                             cudaMemcpyDeviceToHost, b->stream));
+  }
+  MFG_CUDA(cudaMemcpyAsync(o + 6 * N, b->d_vol.p + rve, sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  MFG_CUDA(cudaMemcpyAsync(o + 6 * N + 1, b->d_cur.p + 6 * rve, 6 * sizeof(double),
+                           cudaMemcpyDeviceToHost, b->stream));
+  MFG_CUDA(cudaStreamSynchronize(b->stream));
+  return MFG_OK;
+}
+
+mfg_status mfg_batch_import_state(mfg_batch* b, int32_t rve, const void* buf, size_t bytes) {
+  g_last_error.clear();
+  if (!b || !buf || rve < 0 || rve >= b->R) return fail(MFG_E_INVALID, "bad rve or NULL buffer");
+  if (bytes < mfg_batch_state_bytes(b, rve)) return fail(MFG_E_INVALID, "buffer too small");
+  MFG_CUDA(cudaSetDevice(b->device));
+  const mfg::RveDesc& d = b->desc[rve];
+  const size_t N = d.n_nodes;
+  const double* o = static_cast<const double*>(buf);
+  for (size_t k = 0; k < 6 * N + 7; ++k)
+    if (!std::isfinite(o[k])) return fail(MFG_E_INVALID, "state holds a non-finite value");
+  for (int k = 0; k < 3; ++k) {
+    MFG_CUDA(cudaMemcpyAsync(b->d_u.p + k * b->nt + d.node_off, o + k * N, N * sizeof(double),
+                             cudaMemcpyHostToDevice, b->stream));
+    MFG_CUDA(cudaMemcpyAsync(b->d_x.p + k * b->nt + d.node_off, o + (3 + k) * N, N * sizeof(double),
+                             cudaMemcpyHostToDevice, b->stream));
+  }
+  MFG_CUDA(cudaMemcpyAsync(b->d_vol.p + rve, o + 6 * N, sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  MFG_CUDA(cudaMemcpyAsync(b->d_cur.p + 6 * rve, o + 6 * N + 1, 6 * sizeof(double),
+                           cudaMemcpyHostToDevice, b->stream));
+  MFG_CUDA(cudaStreamSynchronize(b->stream));
+  return MFG_OK;
+}
+
+mfg_status mfg_batch_last_timing(mfg_batch* b, float* relax_ms, float* run_ms) {
+  g_last_error.clear();
+  if (!b) return fail(MFG_E_INVALID, "NULL batch");
+  if (!b->timing_valid) return fail(MFG_E_INVALID, "no completed run to time");
+  MFG_CUDA(cudaSetDevice(b->device));
+  MFG_CUDA(cudaEventSynchronize(b->ev_run1));
+  if (relax_ms) MFG_CUDA(cudaEventElapsedTime(relax_ms, b->ev_relax0, b->ev_relax1));
+  if (run_ms) MFG_CUDA(cudaEventElapsedTime(run_ms, b->ev_run0, b->ev_run1));
+  return MFG_OK;
+}
+
+int32_t mfg_batch_last_launches(const mfg_batch* b) { return b ? b->last_launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,83 @@
+// Internal layout shared by the host library and the CUDA kernels.
+//
+// A batch is packed like the reference's PackedData (PackedData.h:78-175):
+// every per-node array holds all RVEs back to back, and each quantity with
+// three components is stored as three contiguous component blocks of
+// `n_nodes_total` entries (structure of arrays), so a warp reading 32
+// consecutive nodes of one component issues one coalesced transaction.
+// Node ids inside an RVE are the boundary-last order: free nodes
+// [0, n_free), boundary nodes [n_free, n_nodes).
+#ifndef MFG_INTERNAL_H
+#define MFG_INTERNAL_H
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace mfg {
+
+constexpr int kUpdateFreq = 100;  // dt and residual refresh period (TeamOuterLoop.h:4)
+
+struct RveDesc {
+  int64_t node_off;   // first node in the packed node arrays
+  int64_t fiber_off;  // first fiber in the packed fiber arrays
+  int64_t inc_off;    // first entry in the packed CSR incidence array
+  int64_t row_off;    // first entry in the packed CSR row pointer array
+  int64_t bnd_off;    // first boundary node in the packed boundary scratch
+  int32_t n_nodes, n_free, n_fibers, law;
+  int32_t max_steps, mode, pad0, pad1;
+  double E, A, B, lt;  // reaction 0: modulus, area, nonlinear B and transition ratio
+  double c, crit, tol; // strategy
+  double sound_speed;  // sqrt(E / rho)
+  double scale;        // stress scale factor
+};
+
+// Device pointers of one batch, FP64 state.
+struct DevBatch {
+  int32_t n_rve;
+  int64_t nt;  // total nodes
+  int64_t et;  // total fibers
+  const RveDesc* desc;
+  const double* X;   // 3 * nt reference coordinates
+  double* x;         // 3 * nt current coordinates
+  double* u;         // 3 * nt displacement
+  double* v;         // 3 * nt velocity
+  const double* m;   // nt lumped mass
+  const int2* conn;  // et fiber end nodes (RVE-local ids)
+  const double* l0;  // et reference lengths
+  double* nrm;       // 3 * et per-fiber force vectors (scratch)
+  double* fint;      // 3 * nt internal force (boundary rows used by the stress)
+  const int32_t* rowptr;  // per RVE n_nodes + 1 offsets into that RVE's incidences
+  const int32_t* inc;     // 2 * et incidences: (local fiber << 1) | end
+  double* ramp;      // 6 * total boundary nodes: RAMP start and increment
+  double* vol;       // n_rve current volume
+  double* cur_stress;  // n_rve * 6 stress of the last updating run
+  const int32_t* order;  // n_rve RVE ids, most work first
+  int32_t* queue;        // work counter for the persistent launch
+};
+
+struct RunArgs {
+  const double* F;  // device, n_F * 9
+  int32_t n_F;
+  int32_t update_coords;
+  double* sigma;        // device, n_rve * 6
+  int32_t* st_status;   // device, n_rve
+  int32_t* st_steps;    // device, n_rve
+  double* st_residual;  // device, n_rve
+};
+
+// Launchers (mfg_relax_f64.cu). Return cudaGetLastError() of the launch.
+cudaError_t launch_relax_f64(const DevBatch& b, const RunArgs& a, int threads, int grid,
+                             cudaStream_t s);
+int relax_f64_max_blocks_per_sm(int threads);
+
+// Orientation tensors (mfg_aux.cu), omega device n_rve * 9, normal device n_rve * 3
+cudaError_t launch_orientation(const DevBatch& b, const double* normal, double* omega,
+                               cudaStream_t s);
+// Gathers status arrays into mfg_rve_status-shaped records (device).
+cudaError_t launch_pack_status(const int32_t* status, const int32_t* steps,
+                               const double* residual, int n, void* out, cudaStream_t s);
+
+}  // namespace mfg
+
+#endif

@@ -1,0 +1,32 @@
+// Mixed-precision relaxation (FP32 forces and integrator on FP64 reference
+// coordinates plus Kahan-compensated FP32 displacements).
+#ifndef MFG_MIXED_H
+#define MFG_MIXED_H
+
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "mfg_internal.h"
+
+namespace mfg {
+
+struct MixedState;
+MixedState* mixed_new();
+
+// Allocates the mixed-precision working set of a batch.
+cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<RveDesc>& desc,
+                         int sms, cudaStream_t s);
+// One run: reads the persistent FP64 state (x, u, vol), relaxes in mixed
+// precision and writes the FP64 state, stress and status back.
+cudaError_t run_mixed(MixedState& ms, const DevBatch& b, const RunArgs& a, cudaStream_t s,
+                      int* launches);
+void mixed_destroy(MixedState* ms);
+
+struct MixedStateDeleter {
+  void operator()(MixedState* p) const { mixed_destroy(p); }
+};
+
+}  // namespace mfg
+
+#endif
