@@ -199,6 +199,39 @@ size_t mfg_batch_state_bytes(const mfg_batch* batch, int32_t rve);
 mfg_status mfg_batch_export_state(mfg_batch* batch, int32_t rve, void* buf, size_t bytes);
 mfg_status mfg_batch_import_state(mfg_batch* batch, int32_t rve, const void* buf, size_t bytes);
 
+/* ---- solve without allocating ------------------------------------------ */
+/* Size of the device array that mfg_batch_run_device_noalloc() takes its
+ * scratch from (16 MiB). Every GPU that loads this library holds it until the
+ * process exits. */
+#define MFG_NOALLOC_SCRATCH_BYTES (16u << 20)
+
+/* No counterpart in the reference. Same solve as mfg_batch_run_device() on
+ * an FP64 batch, for callers that must not allocate device memory while they
+ * solve: for instance a macroscale code whose device memory is owned by its
+ * own pool allocator (every byte it has not handed out is spoken for), or a
+ * time-stepping loop that forbids allocation after start-up. The call makes no
+ * cudaMalloc/cudaFree and calls no allocating library routine: the kernel's
+ * scratch (per-fiber force vectors, internal forces, RAMP boundary data, the
+ * work counter and the per-RVE status words) comes from one file-scope device
+ * array of MFG_NOALLOC_SCRATCH_BYTES bytes. The caller still passes the
+ * inputs and outputs (device F and sigma, optional device status, as in
+ * mfg_batch_run_device()); the batch keeps the RVE state.
+ *  - Scratch need: 8 * (3 * fibers + 3 * nodes + 6 * boundary nodes) bytes
+ *    over the whole batch plus 16 bytes per RVE (each piece rounded up to 256
+ *    bytes). Larger batches get MFG_E_INVALID with the need in the message.
+ *  - The first call on a device looks up the array's device address (once
+ *    per device, with that device current); make that first call before any
+ *    stream capture.
+ *  - Every call shares the one array: calls whose work overlaps on the GPU
+ *    (other streams, other batches, other host threads) race on it and must
+ *    be serialised by the caller. The array keeps the last call's contents;
+ *    the call clears what must start at zero.
+ *  - MIXED-precision batches are rejected (MFG_E_INVALID).
+ * Returns after enqueueing on `stream` (NULL = the batch's own stream). */
+mfg_status mfg_batch_run_device_noalloc(mfg_batch* batch, const double* F_dev, int32_t n_F,
+                                        double* sigma_dev, int32_t update_coords,
+                                        mfg_rve_status* status_dev, void* stream);
+
 /* ---- timing ----------------------------------------------------------- */
 /* Device time of the last run's relaxation kernel and of the whole run, in
  * milliseconds, from CUDA events recorded on the launching stream. Valid

@@ -69,6 +69,8 @@ def load_library(path: str | None = None):
     L.mfg_batch_run.argtypes = [vp, dp, i32, dp, i32, vp]
     L.mfg_batch_run_device.restype = i32
     L.mfg_batch_run_device.argtypes = [vp, vp, i32, vp, i32, vp, vp]
+    L.mfg_batch_run_device_noalloc.restype = i32
+    L.mfg_batch_run_device_noalloc.argtypes = [vp, vp, i32, vp, i32, vp, vp]
     L.mfg_batch_material_stiffness.restype = i32
     L.mfg_batch_material_stiffness.argtypes = [vp, dp]
     L.mfg_batch_orientation_3d.restype = i32
@@ -242,6 +244,16 @@ class BatchedFiberRVEAnalysisExplicit:
                                                    C.c_void_p(sigma_ptr), int(bool(update_coords)),
                                                    C.c_void_p(status_ptr or None),
                                                    C.c_void_p(stream or None)))
+
+    def run_device_noalloc(self, F_ptr: int, n_F: int, sigma_ptr: int, update_coords: bool = True,
+                           status_ptr: int = 0, stream: int = 0):
+        """mfg_batch_run_device_noalloc(): the FP64 solve of run_device() for
+        callers that must not allocate device memory while solving; the
+        kernel's scratch comes from the library's fixed device array (see
+        include/mumfim_gpu.h for the size limit and the sharing rules)."""
+        _check(load_library().mfg_batch_run_device_noalloc(
+            self._h, C.c_void_p(F_ptr), n_F, C.c_void_p(sigma_ptr), int(bool(update_coords)),
+            C.c_void_p(status_ptr or None), C.c_void_p(stream or None)))
 
     def last_timing(self):
         """(relaxation kernel ms, whole run ms) of the last run, CUDA events."""

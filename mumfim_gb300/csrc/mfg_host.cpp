@@ -576,6 +576,46 @@ mfg_status mfg_batch_run_device(mfg_batch* b, const double* F_dev, int32_t n_F, 
   return MFG_OK;
 }
 
+mfg_status mfg_batch_run_device_noalloc(mfg_batch* b, const double* F_dev, int32_t n_F,
+                                        double* sigma_dev, int32_t update_coords,
+                                        mfg_rve_status* status_dev, void* stream) {
+  g_last_error.clear();
+  if (!b || !F_dev || !sigma_dev) return fail(MFG_E_INVALID, "NULL argument");
+  if (b->precision != MFG_PREC_F64)
+    return fail(MFG_E_INVALID, "the no-allocation solve runs FP64 batches only");
+  mfg_status st = check_run_args(b, n_F, update_coords);
+  if (st != MFG_OK) return st;
+  const size_t need = mfg::relax_f64_static_scratch_bytes(b->dev, b->nbt);
+  if (need > MFG_NOALLOC_SCRATCH_BYTES)
+    return fail(MFG_E_INVALID, "batch needs %zu bytes of scratch, the fixed array holds %u",
+                need, static_cast<unsigned>(MFG_NOALLOC_SCRATCH_BYTES));
+  MFG_CUDA(cudaSetDevice(b->device));
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : b->stream;
+  b->timing_valid = false;
+  MFG_CUDA(cudaEventRecord(b->ev_run0, s));
+  mfg::RunArgs a{};
+  a.F = F_dev;
+  a.n_F = n_F;
+  a.update_coords = update_coords;
+  a.sigma = sigma_dev;
+  MFG_CUDA(cudaEventRecord(b->ev_relax0, s));
+  const int grid = std::min(b->R, b->sms * mfg::relax_f64_max_blocks_per_sm(0));
+  mfg::StaticStatus ss{};
+  cudaError_t e = mfg::launch_relax_f64_static(b->dev, a, grid, b->nbt, s, &ss);
+  if (e != cudaSuccess)
+    return fail(MFG_E_CUDA, "fixed-scratch relaxation launch failed: %s", cudaGetErrorString(e));
+  b->last_launches = 1;
+  MFG_CUDA(cudaEventRecord(b->ev_relax1, s));
+  if (status_dev) {
+    e = mfg::launch_pack_status(ss.status, ss.steps, ss.residual, b->R, status_dev, s);
+    if (e != cudaSuccess) return fail(MFG_E_CUDA, "status pack failed: %s", cudaGetErrorString(e));
+    b->last_launches += 1;
+  }
+  MFG_CUDA(cudaEventRecord(b->ev_run1, s));
+  b->timing_valid = true;
+  return MFG_OK;
+}
+
 mfg_status mfg_batch_run(mfg_batch* b, const double* F, int32_t n_F, double* sigma,
                          int32_t update_coords, mfg_rve_status* status) {
   g_last_error.clear();

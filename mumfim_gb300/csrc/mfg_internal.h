@@ -71,6 +71,18 @@ cudaError_t launch_relax_f64(const DevBatch& b, const RunArgs& a, int threads, i
                              cudaStream_t s);
 int relax_f64_max_blocks_per_sm(int threads);
 
+// Fixed-scratch variant of the FP64 launch (mfg_relax_f64.cu): scratch comes
+// from a file-scope device array of MFG_NOALLOC_SCRATCH_BYTES bytes; no
+// allocation. Returns cudaErrorInvalidValue when the batch needs more scratch.
+struct StaticStatus {
+  int32_t* status;
+  int32_t* steps;
+  double* residual;
+};
+size_t relax_f64_static_scratch_bytes(const DevBatch& b, int64_t n_boundary_total);
+cudaError_t launch_relax_f64_static(const DevBatch& b, const RunArgs& a, int grid,
+                                    int64_t n_boundary_total, cudaStream_t s, StaticStatus* status);
+
 // Orientation tensors (mfg_aux.cu), omega device n_rve * 9, normal device n_rve * 3
 cudaError_t launch_orientation(const DevBatch& b, const double* normal, double* omega,
                                cudaStream_t s);

@@ -28,6 +28,9 @@
 // giving two block barriers per step.
 #include <cfloat>
 #include <climits>
+#include <mutex>
+
+#include "mumfim_gpu.h"
 
 #include "mfg_common.cuh"
 #include "mfg_internal.h"
@@ -338,6 +341,84 @@ int relax_f64_max_blocks_per_sm(int threads) {
       cudaSuccess)
     return 1;
   return n > 0 ? n : 1;
+}
+
+// ---- fixed-scratch variant ---------------------------------------------------
+// The same relaxation kernel, with every scratch buffer it writes (per-fiber
+// force vectors, internal forces, RAMP boundary data, the work counter and the
+// per-RVE status words) carved out of one file-scope device array instead of
+// buffers allocated with the batch. Every GPU that loads this library holds
+// the array until the process exits; all calls on a device share it.
+static __device__ __align__(256) unsigned char g_relax_scratch[MFG_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+void* g_scratch_addr[kMaxDevices] = {};
+
+inline size_t align256(size_t n) { return (n + 255) & ~static_cast<size_t>(255); }
+
+}  // namespace
+
+size_t relax_f64_static_scratch_bytes(const DevBatch& b, int64_t n_boundary_total) {
+  const size_t R = static_cast<size_t>(b.n_rve);
+  return align256(sizeof(int32_t)) + align256(R * sizeof(int32_t)) * 2 +
+         align256(R * sizeof(double)) + align256(3 * static_cast<size_t>(b.et) * sizeof(double)) +
+         align256(3 * static_cast<size_t>(b.nt) * sizeof(double)) +
+         align256(6 * static_cast<size_t>(n_boundary_total > 0 ? n_boundary_total : 1) *
+                  sizeof(double));
+}
+
+cudaError_t launch_relax_f64_static(const DevBatch& batch, const RunArgs& args, int grid,
+                                    int64_t n_boundary_total, cudaStream_t s,
+                                    StaticStatus* status) {
+  if (relax_f64_static_scratch_bytes(batch, n_boundary_total) > MFG_NOALLOC_SCRATCH_BYTES)
+    return cudaErrorInvalidValue;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  unsigned char* base = nullptr;
+  {
+    // Set-up, once per device, with that device current: the host-side
+    // symbol is only a stand-in; the kernel needs the device address.
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_addr[dev]) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_relax_scratch);
+      if (e != cudaSuccess) return e;
+      g_scratch_addr[dev] = p;
+    }
+    base = static_cast<unsigned char*>(g_scratch_addr[dev]);
+  }
+  const size_t R = static_cast<size_t>(batch.n_rve);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    unsigned char* p = base + off;
+    off += align256(bytes);
+    return p;
+  };
+  DevBatch b = batch;
+  RunArgs a = args;
+  b.queue = reinterpret_cast<int32_t*>(take(sizeof(int32_t)));
+  a.st_status = reinterpret_cast<int32_t*>(take(R * sizeof(int32_t)));
+  a.st_steps = reinterpret_cast<int32_t*>(take(R * sizeof(int32_t)));
+  a.st_residual = reinterpret_cast<double*>(take(R * sizeof(double)));
+  b.nrm = reinterpret_cast<double*>(take(3 * static_cast<size_t>(b.et) * sizeof(double)));
+  b.fint = reinterpret_cast<double*>(take(3 * static_cast<size_t>(b.nt) * sizeof(double)));
+  b.ramp = reinterpret_cast<double*>(
+      take(6 * static_cast<size_t>(n_boundary_total > 0 ? n_boundary_total : 1) * sizeof(double)));
+  // The work counter is the only scratch read before it is written.
+  e = cudaMemsetAsync(b.queue, 0, sizeof(int32_t), s);
+  if (e != cudaSuccess) return e;
+  relax_f64_kernel<<<grid, kThreadsF64, 0, s>>>(b, a);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  status->status = a.st_status;
+  status->steps = a.st_steps;
+  status->residual = a.st_residual;
+  return cudaSuccess;
 }
 
 }  // namespace mfg
