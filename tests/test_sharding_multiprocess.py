@@ -1,0 +1,66 @@
+"""Multi-rank path on CPU: two gloo ranks shard a batch of RVEs, solve their
+shards (the CPU oracle stands in for each rank's GPU), and all-gather the
+stresses; the result must equal one process solving the whole batch."""
+import os
+import socket
+
+import numpy as np
+import pytest
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, world, port, q):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        from mumfim_gb300 import sharding
+        from mumfim_gb300 import synthetic as S
+        from oracle import pyoracle
+        w = S.config2(n_rve=6, steps=200, n_min=200, n_max=900)
+        shards = sharding.shard_rves([n.n_fibers for n in w.networks], world)
+        mine = shards[rank]
+        sub = w.subset(mine)
+        rc, sig, st = pyoracle.OracleBatch(sub.networks, sub.strategies).run(sub.F)
+        full = sharding.gather_stress(mine, sig, w.n_rve)
+        q.put((rank, mine, full))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_rank_sharded_solve_equals_single_process(lib_path, oracle):
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=180) for _ in range(2)]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    from mumfim_gb300 import synthetic as S
+    w = S.config2(n_rve=6, steps=200, n_min=200, n_max=900)
+    rc, sig, st = oracle.OracleBatch(w.networks, w.strategies).run(w.F)
+    shards = sorted(r[1] for r in res)
+    assert sorted(sum(shards, [])) == list(range(6)) and all(shards)
+    for rank, mine, full in res:
+        np.testing.assert_array_equal(full, sig)
+
+
+def test_shard_balance():
+    from mumfim_gb300.sharding import shard_rves
+    work = [10, 9, 8, 7, 6, 5, 4, 3, 2, 1]
+    s = shard_rves(work, 3)
+    loads = [sum(work[i] for i in sh) for sh in s]
+    assert sorted(sum(s, [])) == list(range(10))
+    assert max(loads) - min(loads) <= 1
+    with pytest.raises(ValueError):
+        shard_rves(work, 0)
