@@ -1,0 +1,91 @@
+"""Mixed-precision kernel (FP32 forces and integrator, FP64 reference
+coordinates + Kahan-compensated FP32 displacements, FP64 stress / residual /
+dt) against the plain FP64 kernel and the oracle.
+
+Tolerance: 1e-5 relative stress error against FP64 (the target the mixed
+path is specified to), measured as max |sigma_mixed - sigma_f64| over the
+largest |sigma_f64| of the batch.
+"""
+import numpy as np
+import pytest
+
+from conftest import network_2_7, voigt_to_mat
+
+pytestmark = pytest.mark.gpu
+
+REL_MIXED = 1e-5
+
+
+def _rel(a, b):
+    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / np.abs(np.asarray(b)).max())
+
+
+@pytest.fixture(scope="module")
+def M(lib_path):
+    import mumfim_gb300 as m
+    return m
+
+
+def _solve(M, w, precision, **kw):
+    g = M.BatchedFiberRVEAnalysisExplicit(w.networks, w.strategies, precision=precision)
+    sig = np.zeros((w.n_rve, 6))
+    g.run(w.F, sig, **kw)
+    return g, sig
+
+
+def test_mixed_config1_subset_within_1e5_of_f64(M):
+    from mumfim_gb300 import synthetic as S
+    w = S.config1(n_rve=16, steps=5_000)
+    g64, s64 = _solve(M, w, "f64")
+    g32, s32 = _solve(M, w, "mixed")
+    assert (g32.last_status["steps"] == 5_000).all()
+    assert _rel(s32, s64) <= REL_MIXED
+    for r in (0, 9):
+        assert _rel(g32.displacements(r), g64.displacements(r)) <= REL_MIXED
+
+
+def test_mixed_config2_uneven_subset(M):
+    from mumfim_gb300 import synthetic as S
+    w = S.config2(n_rve=12, steps=2_000)
+    g64, s64 = _solve(M, w, "f64")
+    g32, s32 = _solve(M, w, "mixed")
+    assert _rel(s32, s64) <= REL_MIXED
+
+
+def test_mixed_nonlinear_law(M, oracle):
+    from mumfim_gb300 import synthetic as S
+    w = S.config3(n_rve=6, steps=3_000, n_min=500, n_max=1200)
+    g64, s64 = _solve(M, w, "f64")
+    g32, s32 = _solve(M, w, "mixed")
+    assert _rel(s32, s64) <= REL_MIXED
+
+
+def test_mixed_relax_network_2_7(M, golden_2_7):
+    g = golden_2_7
+    net = network_2_7(g)
+    s = M.SolutionStrategy(visc_damp_coeff=g["visc_damp_coeff"], residual_tol=1e-6)
+    gpu = M.BatchedFiberRVEAnalysisExplicit([net], [s], precision="mixed")
+    F = np.array(g["F"]).reshape(1, 3, 3)
+    sig = np.zeros((1, 6))
+    assert gpu.run(F, sig)
+    assert gpu.last_status["steps"][0] % 100 == 1
+    gold = np.array(g["outputs"]["explicit_cpu_out"]["stress"][0])
+    J = np.linalg.det(F[0])
+    assert np.abs(voigt_to_mat(sig[0] * J) - gold).max() <= 1e-5 * np.abs(gold).max()
+
+
+def test_mixed_incremental_and_transactional_runs(M):
+    from mumfim_gb300 import synthetic as S
+    w = S.config1(n_rve=3, n_nodes=700, steps=1_500)
+    a = M.BatchedFiberRVEAnalysisExplicit(w.networks, w.strategies, precision="f64")
+    b = M.BatchedFiberRVEAnalysisExplicit(w.networks, w.strategies, precision="mixed")
+    F2 = np.repeat((np.eye(3) + 0.01 * np.array([[0, 1, 0], [0, 0, 0], [0, 0, -1.0]]))[None], 3, 0)
+    for F, upd in ((w.F, True), (F2, True), (F2[:1], False), (w.F, True)):
+        sa, sb = np.zeros((3, 6)), np.zeros((3, 6))
+        a.run(F, sa, update_coords=upd)
+        b.run(F, sb, update_coords=upd)
+        assert _rel(sb, sa) <= REL_MIXED
+    for r in range(3):
+        assert _rel(b.displacements(r), a.displacements(r)) <= REL_MIXED
+    np.testing.assert_allclose(b.compute3DOrientationTensor(), a.compute3DOrientationTensor(),
+                               rtol=0, atol=1e-9)
