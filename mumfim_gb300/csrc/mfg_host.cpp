@@ -67,13 +67,14 @@ inline double seg_length(const double* a, const double* b) {
 // Host-side product of the set-up of one RVE, solver (boundary-last) order.
 struct RveSetup {
   int n_nodes = 0, n_free = 0, n_fibers = 0;
-  std::vector<int32_t> perm;  // original id -> solver id
+  std::vector<int32_t> perm;  // original id -> storage id
   std::vector<double> X;      // 3 x n_nodes, component blocks
   std::vector<double> m;
   std::vector<int32_t> conn;  // 2 x n_fibers interleaved (n1, n2)
   std::vector<double> l0;
   std::vector<int32_t> rowptr;  // n_nodes + 1
   std::vector<int32_t> inc;     // 2 * n_fibers
+  std::vector<int32_t> bnd_order;  // boundary nodes in the reference's order
   std::string error;
 };
 
@@ -123,20 +124,49 @@ void setup_rve(const mfg_network& net, RveSetup& s) {
     degree[n2]++;
   }
   // boundary-last permutation (BatchedReorderMesh.h:54-73)
-  s.perm.assign(N, 0);
-  for (int i = 0; i < nb; ++i) s.perm[fixed[i]] = i + 1;
+  std::vector<int32_t> ref(N, 0);
+  for (int i = 0; i < nb; ++i) ref[fixed[i]] = i + 1;
   int update = 0;
   for (int i = 0; i < N; ++i) {
-    int val = s.perm[i];
+    int val = ref[i];
     bool is_fixed = val > 0;
     update += is_fixed ? 1 : 0;
-    s.perm[i] = is_fixed ? (N - nb) + (val - 1) : i - update;
+    ref[i] = is_fixed ? (N - nb) + (val - 1) : i - update;
   }
   for (int i = 0; i < N; ++i)
-    if (degree[i] == 0 && s.perm[i] < N - nb) {
+    if (degree[i] == 0 && ref[i] < N - nb) {
       s.error = "free node " + std::to_string(i) + " has no fibers (zero lumped mass)";
       return;
     }
+  // Storage order: still boundary-last, but each segment sorted along a
+  // Morton curve of the reference coordinates, so that a fiber's two end
+  // nodes sit close together in memory. Nothing numerical depends on it:
+  // each node's CSR row keeps the original fiber order and the stress visits
+  // the boundary in the reference's order (bnd_order).
+  auto morton = [&](int i) {
+    uint64_t code = 0;
+    uint32_t q[3];
+    for (int k = 0; k < 3; ++k) {
+      double t = (net.coords[3 * i + k] + 0.5) * 1024.0;
+      q[k] = static_cast<uint32_t>(t < 0 ? 0 : (t > 1023 ? 1023 : t));
+    }
+    for (int bit = 9; bit >= 0; --bit)
+      for (int k = 0; k < 3; ++k) code = (code << 1) | ((q[k] >> bit) & 1u);
+    return code;
+  };
+  std::vector<int32_t> by_ref(N);
+  for (int i = 0; i < N; ++i) by_ref[ref[i]] = i;  // reference order -> original id
+  std::vector<uint64_t> key(N);
+  for (int i = 0; i < N; ++i) key[i] = morton(i);
+  std::vector<int32_t> store(by_ref);
+  std::stable_sort(store.begin(), store.begin() + (N - nb),
+                   [&](int a, int b) { return key[a] < key[b]; });
+  std::stable_sort(store.begin() + (N - nb), store.end(),
+                   [&](int a, int b) { return key[a] < key[b]; });
+  s.perm.assign(N, 0);
+  for (int j = 0; j < N; ++j) s.perm[store[j]] = j;
+  s.bnd_order.resize(nb);
+  for (int k = 0; k < nb; ++k) s.bnd_order[k] = s.perm[by_ref[N - nb + k]];
   s.n_nodes = N;
   s.n_free = N - nb;
   s.n_fibers = E;
@@ -147,26 +177,42 @@ void setup_rve(const mfg_network& net, RveSetup& s) {
     for (int k = 0; k < 3; ++k) s.X[static_cast<size_t>(k) * N + p] = net.coords[3 * i + k];
     s.m[p] = mass[i];
   }
+  // fiber slots ordered by their lower end node, then the other end
+  std::vector<int32_t> slot_fiber(E);
+  std::iota(slot_fiber.begin(), slot_fiber.end(), 0);
+  auto ends = [&](int e) {
+    int a = s.perm[net.connectivity[2 * e]], b = s.perm[net.connectivity[2 * e + 1]];
+    return std::make_pair(std::min(a, b), std::max(a, b));
+  };
+  std::stable_sort(slot_fiber.begin(), slot_fiber.end(),
+                   [&](int x, int y) { return ends(x) < ends(y); });
+  std::vector<int32_t> fiber_slot(E);
+  for (int j = 0; j < E; ++j) fiber_slot[slot_fiber[j]] = j;
   s.conn.resize(2 * static_cast<size_t>(E));
   s.l0.resize(E);
   std::vector<int32_t> cnt(N + 1, 0);
-  for (int e = 0; e < E; ++e) {
+  for (int j = 0; j < E; ++j) {
+    const int e = slot_fiber[j];
     int a = s.perm[net.connectivity[2 * e]], b = s.perm[net.connectivity[2 * e + 1]];
-    s.conn[2 * e] = a;
-    s.conn[2 * e + 1] = b;
+    s.conn[2 * j] = a;
+    s.conn[2 * j + 1] = b;
     double pa[3] = {s.X[a], s.X[N + a], s.X[2 * static_cast<size_t>(N) + a]};
     double pb[3] = {s.X[b], s.X[N + b], s.X[2 * static_cast<size_t>(N) + b]};
-    s.l0[e] = seg_length(pa, pb);
+    s.l0[j] = seg_length(pa, pb);
     cnt[a + 1]++;
     cnt[b + 1]++;
   }
-  // CSR incidence: fibers in ascending id per node; end 0 = first node.
+  // CSR incidence: per node, fibers in ascending ORIGINAL id (the serial
+  // scatter order), stored as (slot << 1) | end with end 0 = first node.
   s.rowptr.assign(N + 1, 0);
   for (int i = 0; i < N; ++i) s.rowptr[i + 1] = s.rowptr[i] + cnt[i + 1];
   s.inc.resize(2 * static_cast<size_t>(E));
   std::vector<int32_t> fill(s.rowptr.begin(), s.rowptr.end() - 1);
   for (int e = 0; e < E; ++e)
-    for (int j = 0; j < 2; ++j) s.inc[fill[s.conn[2 * e + j]]++] = (e << 1) | j;
+    for (int j = 0; j < 2; ++j) {
+      const int node = s.perm[net.connectivity[2 * e + j]];
+      s.inc[fill[node]++] = (fiber_slot[e] << 1) | j;
+    }
 }
 
 template <typename Fn>
@@ -219,7 +265,7 @@ struct mfg_batch {
   DevArray<mfg::RveDesc> d_desc;
   DevArray<double> d_X, d_x, d_u, d_v, d_m, d_l0, d_nrm, d_fint, d_ramp, d_vol, d_cur;
   DevArray<int2> d_conn;
-  DevArray<int32_t> d_rowptr, d_inc, d_order, d_queue;
+  DevArray<int32_t> d_rowptr, d_inc, d_bnd, d_order, d_queue;
   // per-run scratch
   DevArray<double> d_F, d_sigma, d_res, d_omega;
   DevArray<int32_t> d_status, d_steps;
@@ -235,7 +281,8 @@ struct mfg_batch {
       a->release();
     d_desc.release();
     d_conn.release();
-    for (auto* a : {&d_rowptr, &d_inc, &d_order, &d_queue, &d_status, &d_steps}) a->release();
+    for (auto* a : {&d_rowptr, &d_inc, &d_bnd, &d_order, &d_queue, &d_status, &d_steps})
+      a->release();
     d_st.release();
     for (auto* e : {&ev_run0, &ev_relax0, &ev_relax1, &ev_run1})
       if (*e) cudaEventDestroy(*e);
@@ -450,7 +497,7 @@ mfg_status mfg_batch_create(const mfg_network* nets, const mfg_strategy* strateg
   // ---- pack ------------------------------------------------------------
   std::vector<double> X(3 * nt), m(nt), l0(et);
   std::vector<int2> conn(et);
-  std::vector<int32_t> rowptr(ro), inc(io);
+  std::vector<int32_t> rowptr(ro), inc(io), bnd(std::max<int64_t>(bo, 1));
   parallel_for(n_rve, [&](int r) {
     const RveSetup& s = su[r];
     const mfg::RveDesc& d = b->desc[r];
@@ -462,6 +509,8 @@ mfg_status mfg_batch_create(const mfg_network* nets, const mfg_strategy* strateg
     std::memcpy(&l0[d.fiber_off], s.l0.data(), s.n_fibers * sizeof(double));
     std::memcpy(&rowptr[d.row_off], s.rowptr.data(), (N + 1) * sizeof(int32_t));
     std::memcpy(&inc[d.inc_off], s.inc.data(), 2 * s.n_fibers * sizeof(int32_t));
+    if (!s.bnd_order.empty())
+      std::memcpy(&bnd[d.bnd_off], s.bnd_order.data(), s.bnd_order.size() * sizeof(int32_t));
   });
   // persistent-queue order: most fibers first (longest-processing-time first)
   std::vector<int32_t> order(n_rve);
@@ -492,6 +541,7 @@ mfg_status mfg_batch_create(const mfg_network* nets, const mfg_strategy* strateg
   MFG_CUDA(b->d_nrm.alloc(3 * et));
   if ((st = upload(b->d_rowptr, rowptr, s)) != MFG_OK) return st;
   if ((st = upload(b->d_inc, inc, s)) != MFG_OK) return st;
+  if ((st = upload(b->d_bnd, bnd, s)) != MFG_OK) return st;
   MFG_CUDA(b->d_ramp.alloc(6 * std::max<int64_t>(b->nbt, 1)));
   std::vector<double> ones(n_rve, 1.0);  // BatchedFiberRVEAnalysisExplicit.h:115-118
   if ((st = upload(b->d_vol, ones, s)) != MFG_OK) return st;
@@ -523,6 +573,7 @@ mfg_status mfg_batch_create(const mfg_network* nets, const mfg_strategy* strateg
   dv.fint = b->d_fint.p;
   dv.rowptr = b->d_rowptr.p;
   dv.inc = b->d_inc.p;
+  dv.bnd = b->d_bnd.p;
   dv.ramp = b->d_ramp.p;
   dv.vol = b->d_vol.p;
   dv.cur_stress = b->d_cur.p;

@@ -5,8 +5,10 @@
 // three components is stored as three contiguous component blocks of
 // `n_nodes_total` entries (structure of arrays), so a warp reading 32
 // consecutive nodes of one component issues one coalesced transaction.
-// Node ids inside an RVE are the boundary-last order: free nodes
-// [0, n_free), boundary nodes [n_free, n_nodes).
+// Node ids inside an RVE are boundary-last: free nodes [0, n_free), boundary
+// nodes [n_free, n_nodes); each segment is sorted along a Morton curve of the
+// reference coordinates for locality. `bnd` lists the boundary nodes in the
+// reference's boundary order, which the stress sum follows.
 #ifndef MFG_INTERNAL_H
 #define MFG_INTERNAL_H
 
@@ -48,7 +50,8 @@ struct DevBatch {
   double* nrm;       // 3 * et per-fiber force vectors (scratch)
   double* fint;      // 3 * nt internal force (boundary rows used by the stress)
   const int32_t* rowptr;  // per RVE n_nodes + 1 offsets into that RVE's incidences
-  const int32_t* inc;     // 2 * et incidences: (local fiber << 1) | end
+  const int32_t* inc;     // 2 * et incidences: (local fiber slot << 1) | end
+  const int32_t* bnd;     // total boundary nodes: local ids in the reference's boundary order
   double* ramp;      // 6 * total boundary nodes: RAMP start and increment
   double* vol;       // n_rve current volume
   double* cur_stress;  // n_rve * 6 stress of the last updating run

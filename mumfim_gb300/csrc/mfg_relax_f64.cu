@@ -280,7 +280,9 @@ __device__ void solve_rve(const DevBatch& b, const RunArgs& a, int rve, double* 
   if (tid < 6) {
     double s = 0.0;
     const int k = tid;
-    for (int i = NF; i < N; ++i) {
+    const int32_t* bo = b.bnd + d.bnd_off;
+    for (int q = 0; q < N - NF; ++q) {
+      const int i = bo[q];
       const double f1 = r.fi0[i], f2 = r.fi1[i], f3 = r.fi2[i];
       const double crd1 = r.x0[i], crd2 = r.x1[i], crd3 = r.x2[i];
       double t;

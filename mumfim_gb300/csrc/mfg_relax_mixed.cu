@@ -18,6 +18,15 @@
 //    reference reduces over the whole RVE.
 // The persistent FP64 state of the batch (x, u, volume) is read at the
 // start and written at the end of every run, so both precisions share it.
+//
+// Memory placement, chosen per RVE inside one persistent launch (one CTA of
+// 512 threads per SM, up to 220 KB of dynamic shared memory):
+//   RESIDENT_ALL  u_hi, u_lo (24 B/node) and the per-fiber force vectors
+//                 (16 B/fiber) live in shared memory for the whole solve;
+//   RESIDENT_NODE only u_hi, u_lo in shared memory, force vectors in global;
+//   STREAM        everything in global memory (L2 / HBM).
+// Per-fiber constants (end nodes, reference vector dX, 1/l0) and per-node
+// constants / velocities always stream from global with coalesced loads.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -30,28 +39,26 @@
 namespace mfg {
 
 struct MixedState {
-  float* u_hi = nullptr;  // 3 * nt
-  float* u_lo = nullptr;  // 3 * nt
-  float* v = nullptr;     // 3 * nt
-  float* minv = nullptr;  // nt, 1 / m
-  float* m32 = nullptr;   // nt
-  float* dX = nullptr;    // 3 * et reference fiber vectors X[n2] - X[n1]
-  float* rl0 = nullptr;   // et, 1 / l0
-  float* nrm = nullptr;   // 3 * et per-fiber force vectors (scratch)
+  float* u_hi = nullptr;   // 3 * nt (STREAM placement)
+  float* u_lo = nullptr;   // 3 * nt
+  float4* v = nullptr;     // nt, velocity (w unused)
+  float2* mass = nullptr;  // nt, (1 / m, m)
+  float4* fcon = nullptr;  // et, (X[n2] - X[n1], 1 / l0)
+  float4* nrm = nullptr;   // et, per-fiber force vectors (scratch; w unused)
   int sms = 1;
-  int occ = 1;
+  int smem_bytes = 0;
 };
 
 namespace {
 
 constexpr int kThreadsMixed = 512;
+constexpr int kSmemBytesMixed = 220 * 1024;
 
 __global__ void mixed_prepare_kernel(const DevBatch b, MixedState ms) {
   const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   if (i < b.nt) {
     const double m = b.m[i];
-    ms.m32[i] = static_cast<float>(m);
-    ms.minv[i] = static_cast<float>(1.0 / m);
+    ms.mass[i] = make_float2(static_cast<float>(1.0 / m), static_cast<float>(m));
   }
 }
 
@@ -62,56 +69,20 @@ __global__ void mixed_prepare_fibers_kernel(const DevBatch b, MixedState ms) {
     if (e >= d.n_fibers) continue;
     const int64_t fo = d.fiber_off + e, no = d.node_off;
     const int2 c = b.conn[fo];
+    float dx[3];
     for (int k = 0; k < 3; ++k) {
       const double* X = b.X + k * b.nt + no;
-      ms.dX[k * b.et + fo] = static_cast<float>(X[c.y] - X[c.x]);
+      dx[k] = static_cast<float>(X[c.y] - X[c.x]);
     }
-    ms.rl0[fo] = static_cast<float>(1.0 / b.l0[fo]);
+    ms.fcon[fo] = make_float4(dx[0], dx[1], dx[2], static_cast<float>(1.0 / b.l0[fo]));
   }
-}
-
-struct MixedView {
-  const double *X0, *X1, *X2;
-  double *x0, *x1, *x2, *u0, *u1, *u2;
-  float *h0, *h1, *h2, *lo0, *lo1, *lo2, *v0, *v1, *v2;
-  const float *minv, *m32;
-  const int2* conn;
-  const float *dX0, *dX1, *dX2, *rl0;
-  float *n0, *n1, *n2;
-  double *fi0, *fi1, *fi2;
-  const int32_t* rowptr;
-  const int32_t* inc;
-  double* ramp;
-};
-
-__device__ __forceinline__ MixedView make_view(const DevBatch& b, const MixedState& ms,
-                                               const RveDesc& d) {
-  MixedView r;
-  const int64_t nt = b.nt, et = b.et, no = d.node_off, fo = d.fiber_off;
-  r.X0 = b.X + no; r.X1 = b.X + nt + no; r.X2 = b.X + 2 * nt + no;
-  r.x0 = b.x + no; r.x1 = b.x + nt + no; r.x2 = b.x + 2 * nt + no;
-  r.u0 = b.u + no; r.u1 = b.u + nt + no; r.u2 = b.u + 2 * nt + no;
-  r.h0 = ms.u_hi + no; r.h1 = ms.u_hi + nt + no; r.h2 = ms.u_hi + 2 * nt + no;
-  r.lo0 = ms.u_lo + no; r.lo1 = ms.u_lo + nt + no; r.lo2 = ms.u_lo + 2 * nt + no;
-  r.v0 = ms.v + no; r.v1 = ms.v + nt + no; r.v2 = ms.v + 2 * nt + no;
-  r.minv = ms.minv + no;
-  r.m32 = ms.m32 + no;
-  r.conn = b.conn + fo;
-  r.dX0 = ms.dX + fo; r.dX1 = ms.dX + et + fo; r.dX2 = ms.dX + 2 * et + fo;
-  r.rl0 = ms.rl0 + fo;
-  r.n0 = ms.nrm + fo; r.n1 = ms.nrm + et + fo; r.n2 = ms.nrm + 2 * et + fo;
-  r.fi0 = b.fint + no; r.fi1 = b.fint + nt + no; r.fi2 = b.fint + 2 * nt + no;
-  r.rowptr = b.rowptr + d.row_off;
-  r.inc = b.inc + d.inc_off;
-  r.ramp = b.ramp + 6 * d.bnd_off;
-  return r;
 }
 
 // Per-RVE constants of the fiber law in the T/l form used here.
 struct Law {
   int nonlinear;
   float ea;      // E A
-  float ea_b;    // E A / B            (toe:  T/l = (E A / B / l0) expm1(B g))
+  float ea_b;    // alpha = E A / B (toe: T/l = alpha expm1(B g) / l0)
   float B;
   float lt;      // transition stretch
   float Mt, bt;  // linear continuation T = Mt (lambda - lt) + bt above lt
@@ -168,64 +139,139 @@ __device__ __forceinline__ void comp_add(float& hi, float& lo, float inc) {
   hi = s;
 }
 
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bp = s - a;
+  const float ap = s - bp;
+  e = (a - ap) + (b - bp);
+}
+
 __device__ __forceinline__ void split(double u, float& hi, float& lo) {
   hi = static_cast<float>(u);
   lo = static_cast<float>(u - static_cast<double>(hi));
 }
 
-__device__ __forceinline__ void gather_f32(const MixedView& r, int i, float& a0, float& a1,
-                                           float& a2) {
+// A three-component float field: component k of node/fiber i at p[k*s + i].
+struct Field3 {
+  float* p;
+  int64_t s;
+  __device__ __forceinline__ float& operator()(int k, int i) const { return p[k * s + i]; }
+};
+
+struct Rve {
+  RveDesc d;
+  Law L;
+  Field3 hi, lo;        // node displacement (hi, lo)
+  float4* n;            // fiber force vectors
+  float4* v;            // node velocity (global)
+  const float2* mass;   // (1 / m, m)
+  const float4* fcon;   // (dX, 1 / l0)
+  const int2* conn;
+  const int32_t* rowptr;
+  const int32_t* inc;
+  float* ramp;          // per boundary node: u0_hi[3], u0_lo[3], d[3]
+  int64_t node_off, nt;
+};
+
+// Nodal internal force: incident fiber vectors, signed by the node's end.
+// The first kGatherWidth incidences are loaded with independent, predicated
+// loads so that a thread has all of them in flight at once (rows of a kNN
+// network hold ~2k entries); longer rows finish in a loop.
+constexpr int kGatherWidth = 8;
+
+__device__ __forceinline__ void gather(const Rve& r, int i, float& a0, float& a1, float& a2) {
   a0 = 0.f; a1 = 0.f; a2 = 0.f;
-  const int pb = r.rowptr[i], pe = r.rowptr[i + 1];
-  for (int p = pb; p < pe; ++p) {
-    const int code = __ldg(r.inc + p);
-    const int e = code >> 1;
-    const float s = (code & 1) ? 1.f : -1.f;
-    a0 = fmaf(s, r.n0[e], a0);
-    a1 = fmaf(s, r.n1[e], a1);
-    a2 = fmaf(s, r.n2[e], a2);
+  const int pb = __ldg(r.rowptr + i), pe = __ldg(r.rowptr + i + 1);
+  const int n = pe - pb;
+  int code[kGatherWidth];
+#pragma unroll
+  for (int j = 0; j < kGatherWidth; ++j) code[j] = (j < n) ? __ldg(r.inc + pb + j) : 0;
+  float4 t[kGatherWidth];
+#pragma unroll
+  for (int j = 0; j < kGatherWidth; ++j)
+    if (j < n) t[j] = r.n[code[j] >> 1];
+#pragma unroll
+  for (int j = 0; j < kGatherWidth; ++j) {
+    if (j < n) {
+      const float s = (code[j] & 1) ? 1.f : -1.f;
+      a0 = fmaf(s, t[j].x, a0);
+      a1 = fmaf(s, t[j].y, a1);
+      a2 = fmaf(s, t[j].z, a2);
+    }
+  }
+  for (int p = pb + kGatherWidth; p < pe; ++p) {
+    const int c = __ldg(r.inc + p);
+    const float4 tv = r.n[c >> 1];
+    const float s = (c & 1) ? 1.f : -1.f;
+    a0 = fmaf(s, tv.x, a0);
+    a1 = fmaf(s, tv.y, a1);
+    a2 = fmaf(s, tv.z, a2);
   }
 }
 
-// Fiber pass in FP32; every UPDATE_FREQ steps also the FP64 lengths for
-// dt_crit. Returns the thread's minimum FP64 length (DBL_MAX otherwise).
-__device__ __forceinline__ double fiber_pass_mixed(const MixedView& r, const RveDesc& d,
-                                                   const Law& L, bool want_lmin) {
-  double lmin = DBL_MAX;
-  for (int e = threadIdx.x; e < d.n_fibers; e += kThreadsMixed) {
-    const int2 c = __ldg(r.conn + e);
-    const float du0 = (r.h0[c.y] - r.h0[c.x]) + (r.lo0[c.y] - r.lo0[c.x]);
-    const float du1 = (r.h1[c.y] - r.h1[c.x]) + (r.lo1[c.y] - r.lo1[c.x]);
-    const float du2 = (r.h2[c.y] - r.h2[c.x]) + (r.lo2[c.y] - r.lo2[c.x]);
-    const float X0 = __ldg(r.dX0 + e), X1 = __ldg(r.dX1 + e), X2 = __ldg(r.dX2 + e);
-    const float rl0 = __ldg(r.rl0 + e);
-    const float dxdu = fmaf(X0, du0, fmaf(X1, du1, X2 * du2));
-    const float dudu = fmaf(du0, du0, fmaf(du1, du1, du2 * du2));
-    const float g = fmaf(0.5f, dudu, dxdu) * (rl0 * rl0);
-    const float t = tension_over_length(L, g, rl0);
-    r.n0[e] = (X0 + du0) * t;
-    r.n1[e] = (X1 + du1) * t;
-    r.n2[e] = (X2 + du2) * t;
-    if (want_lmin) {
-      const double a0 = (r.X0[c.y] + (static_cast<double>(r.h0[c.y]) + r.lo0[c.y])) -
-                        (r.X0[c.x] + (static_cast<double>(r.h0[c.x]) + r.lo0[c.x]));
-      const double a1 = (r.X1[c.y] + (static_cast<double>(r.h1[c.y]) + r.lo1[c.y])) -
-                        (r.X1[c.x] + (static_cast<double>(r.h1[c.x]) + r.lo1[c.x]));
-      const double a2 = (r.X2[c.y] + (static_cast<double>(r.h2[c.y]) + r.lo2[c.y])) -
-                        (r.X2[c.x] + (static_cast<double>(r.h2[c.x]) + r.lo2[c.x]));
-      lmin = fmin(lmin, sqrt(a0 * a0 + a1 * a1 + a2 * a2));
-    }
+__device__ __forceinline__ void fiber_force(const Rve& r, int e) {
+  const int2 c = __ldg(r.conn + e);
+  const float du0 = (r.hi(0, c.y) - r.hi(0, c.x)) + (r.lo(0, c.y) - r.lo(0, c.x));
+  const float du1 = (r.hi(1, c.y) - r.hi(1, c.x)) + (r.lo(1, c.y) - r.lo(1, c.x));
+  const float du2 = (r.hi(2, c.y) - r.hi(2, c.x)) + (r.lo(2, c.y) - r.lo(2, c.x));
+  const float4 fc = __ldg(r.fcon + e);
+  const float X0 = fc.x, X1 = fc.y, X2 = fc.z, rl0 = fc.w;
+  const float dxdu = fmaf(X0, du0, fmaf(X1, du1, X2 * du2));
+  const float dudu = fmaf(du0, du0, fmaf(du1, du1, du2 * du2));
+  const float g = fmaf(0.5f, dudu, dxdu) * (rl0 * rl0);
+  const float t = tension_over_length(r.L, g, rl0);
+  r.n[e] = make_float4((X0 + du0) * t, (X1 + du1) * t, (X2 + du2) * t, 0.f);
+}
+
+// FP64 length of one fiber in the current configuration.
+__device__ __forceinline__ double length64(const Rve& r, const double* X, int e) {
+  const int2 c = __ldg(r.conn + e);
+  double s2 = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double* Xk = X + k * r.nt + r.node_off;
+    const double a = Xk[c.x] + (static_cast<double>(r.hi(k, c.x)) + r.lo(k, c.x));
+    const double bq = Xk[c.y] + (static_cast<double>(r.hi(k, c.y)) + r.lo(k, c.y));
+    s2 += (bq - a) * (bq - a);
   }
-  return lmin;
+  return sqrt(s2);
 }
 
 __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const RunArgs& a, int rve,
-                                double* red) {
-  const RveDesc d = b.desc[rve];
-  const MixedView r = make_view(b, ms, d);
-  const Law L = make_law(d);
-  const int N = d.n_nodes, NF = d.n_free;
+                                double* red, float* smem, int smem_floats) {
+  Rve r;
+  r.d = b.desc[rve];
+  const RveDesc& d = r.d;
+  r.L = make_law(d);
+  const int N = d.n_nodes, NF = d.n_free, E = d.n_fibers;
   const int tid = threadIdx.x;
+  const int64_t no = d.node_off, fo = d.fiber_off, nt = b.nt, et = b.et;
+  r.node_off = no;
+  r.nt = nt;
+  // placement
+  // force vectors first (16-byte aligned), then the node fields
+  const int64_t node_floats = 6LL * N, all_floats = 6LL * N + 4LL * E;
+  if (all_floats <= smem_floats) {
+    r.n = reinterpret_cast<float4*>(smem);
+    r.hi = {smem + 4 * E, N};
+    r.lo = {smem + 4 * E + 3 * N, N};
+  } else if (node_floats <= smem_floats) {
+    r.n = ms.nrm + fo;
+    r.hi = {smem, N};
+    r.lo = {smem + 3 * N, N};
+  } else {
+    r.n = ms.nrm + fo;
+    r.hi = {ms.u_hi + no, nt};
+    r.lo = {ms.u_lo + no, nt};
+  }
+  (void)et;
+  r.v = ms.v + no;
+  r.mass = ms.mass + no;
+  r.fcon = ms.fcon + fo;
+  r.conn = b.conn + fo;
+  r.rowptr = b.rowptr + d.row_off;
+  r.inc = b.inc + d.inc_off;
+  r.ramp = reinterpret_cast<float*>(b.ramp + 6 * d.bnd_off);  // 12 floats per boundary node
   const double* F = a.F + 9 * (a.n_F > 1 ? rve : 0);
   const bool ramp = d.mode == 1;
   double Fm[9];
@@ -235,33 +281,53 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
 
   // ---- prologue in FP64: predictor, split into (hi, lo), v = 0 -------------
   for (int i = tid; i < N; i += kThreadsMixed) {
-    const double xo0 = r.x0[i], xo1 = r.x1[i], xo2 = r.x2[i];
-    double up0 = r.u0[i], up1 = r.u1[i], up2 = r.u2[i];
-    if (!ramp) {
-      up0 = (Fm[0] - 1) * xo0 + Fm[1] * xo1 + Fm[2] * xo2 + up0;
-      up1 = Fm[3] * xo0 + (Fm[4] - 1) * xo1 + Fm[5] * xo2 + up1;
-      up2 = Fm[6] * xo0 + Fm[7] * xo1 + (Fm[8] - 1) * xo2 + up2;
+    double xo[3], up[3], X[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      xo[k] = b.x[k * nt + no + i];
+      up[k] = b.u[k * nt + no + i];
+      X[k] = b.X[k * nt + no + i];
     }
-    const double X0 = r.X0[i], X1 = r.X1[i], X2 = r.X2[i];
-    const double xn0 = X0 + up0, xn1 = X1 + up1, xn2 = X2 + up2;
-    float hi, lo;
-    split(xn0 - X0, hi, lo); r.h0[i] = hi; r.lo0[i] = lo;
-    split(xn1 - X1, hi, lo); r.h1[i] = hi; r.lo1[i] = lo;
-    split(xn2 - X2, hi, lo); r.h2[i] = hi; r.lo2[i] = lo;
-    r.v0[i] = 0.f; r.v1[i] = 0.f; r.v2[i] = 0.f;
+    if (!ramp) {
+      const double u0 = (Fm[0] - 1) * xo[0] + Fm[1] * xo[1] + Fm[2] * xo[2] + up[0];
+      const double u1 = Fm[3] * xo[0] + (Fm[4] - 1) * xo[1] + Fm[5] * xo[2] + up[1];
+      const double u2 = Fm[6] * xo[0] + Fm[7] * xo[1] + (Fm[8] - 1) * xo[2] + up[2];
+      up[0] = u0; up[1] = u1; up[2] = u2;
+    }
+    double xn[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      xn[k] = X[k] + up[k];
+      float hi, lo;
+      split(xn[k] - X[k], hi, lo);
+      r.hi(k, i) = hi;
+      r.lo(k, i) = lo;
+    }
+    r.v[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (ramp && i >= NF) {
-      double* rb = r.ramp + 6 * (i - NF);
-      rb[0] = xn0; rb[1] = xn1; rb[2] = xn2;
-      rb[3] = (Fm[0] - 1) * xn0 + Fm[1] * xn1 + Fm[2] * xn2;
-      rb[4] = Fm[3] * xn0 + (Fm[4] - 1) * xn1 + Fm[5] * xn2;
-      rb[5] = Fm[6] * xn0 + Fm[7] * xn1 + (Fm[8] - 1) * xn2;
+      float* rb = r.ramp + 12 * (i - NF);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        rb[k] = r.hi(k, i);
+        rb[3 + k] = r.lo(k, i);
+        rb[6 + k] = static_cast<float>((Fm[3 * k + 0] - (k == 0)) * xn[0] +
+                                       (Fm[3 * k + 1] - (k == 1)) * xn[1] +
+                                       (Fm[3 * k + 2] - (k == 2)) * xn[2]);
+      }
     }
   }
   __syncthreads();
-  double dt_crit = block_min<kThreadsMixed>(fiber_pass_mixed(r, d, L, true), red) / d.sound_speed;
+  double lmin = DBL_MAX;
+  for (int e = tid; e < E; e += kThreadsMixed) {
+    fiber_force(r, e);
+    lmin = fmin(lmin, length64(r, b.X, e));
+  }
+  double dt_crit = block_min<kThreadsMixed>(lmin, red) / d.sound_speed;
 
   const int cap = d.max_steps;
   const float c = static_cast<float>(d.c);
+  const float inv_steps = 1.f / static_cast<float>(d.max_steps);
+  float h_cur = static_cast<float>(d.crit * dt_crit * 0.5);
   int step = 0;
   double residual = 10.0;
   float h_prev = 0.f;
@@ -272,7 +338,7 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
       double part = 0.0;
       for (int i = tid; i < NF; i += kThreadsMixed) {
         float a0, a1, a2;
-        gather_f32(r, i, a0, a1, a2);
+        gather(r, i, a0, a1, a2);
         part += static_cast<double>(a0) * a0 + static_cast<double>(a1) * a1 +
                 static_cast<double>(a2) * a2;
       }
@@ -284,44 +350,60 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
     }
     if (!ramp && res_step && !(residual > d.tol)) break;
     if (step >= cap) break;
-    const double hd = d.crit * dt_crit * 0.5;
-    const float h = static_cast<float>(hd);
+    // per-step scalars in FP32 (h changes only when dt_crit does)
+    const float h = h_cur;
     const float hk = h_prev + h;  // trailing kick of step-1 + leading kick of step
-    const float h2 = static_cast<float>(2.0 * hd);
+    const float h2 = h + h;
     for (int i = tid; i < NF; i += kThreadsMixed) {
-      float a0, a1, a2;
-      gather_f32(r, i, a0, a1, a2);
-      const float mi = r.minv[i];
-      const float mc = r.m32[i] * c;
-      float w0 = r.v0[i], w1 = r.v1[i], w2 = r.v2[i];
-      const float f0 = -a0 - mc * w0;
-      const float f1 = -a1 - mc * w1;
-      const float f2 = -a2 - mc * w2;
-      w0 = fmaf(hk * mi, f0, w0);
-      w1 = fmaf(hk * mi, f1, w1);
-      w2 = fmaf(hk * mi, f2, w2);
-      r.v0[i] = w0; r.v1[i] = w1; r.v2[i] = w2;
-      float hi, lo;
-      hi = r.h0[i]; lo = r.lo0[i]; comp_add(hi, lo, h2 * w0); r.h0[i] = hi; r.lo0[i] = lo;
-      hi = r.h1[i]; lo = r.lo1[i]; comp_add(hi, lo, h2 * w1); r.h1[i] = hi; r.lo1[i] = lo;
-      hi = r.h2[i]; lo = r.lo2[i]; comp_add(hi, lo, h2 * w2); r.h2[i] = hi; r.lo2[i] = lo;
+      float f[3];
+      gather(r, i, f[0], f[1], f[2]);
+      const float2 mm = __ldg(r.mass + i);
+      const float mc = mm.y * c;
+      const float km = hk * mm.x;
+      float4 w = r.v[i];
+      w.x = fmaf(km, -f[0] - mc * w.x, w.x);
+      w.y = fmaf(km, -f[1] - mc * w.y, w.y);
+      w.z = fmaf(km, -f[2] - mc * w.z, w.z);
+      r.v[i] = w;
+      const float wk[3] = {w.x, w.y, w.z};
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        float hi = r.hi(k, i), lo = r.lo(k, i);
+        comp_add(hi, lo, h2 * wk[k]);
+        r.hi(k, i) = hi;
+        r.lo(k, i) = lo;
+      }
     }
     if (ramp) {
-      const double alpha = static_cast<double>(step + 1) / static_cast<double>(d.max_steps);
+      const float alpha = static_cast<float>(step + 1) * inv_steps;
       for (int i = NF + tid; i < N; i += kThreadsMixed) {
-        const double* rb = r.ramp + 6 * (i - NF);
-        float hi, lo;
-        split((rb[0] + alpha * rb[3]) - r.X0[i], hi, lo); r.h0[i] = hi; r.lo0[i] = lo;
-        split((rb[1] + alpha * rb[4]) - r.X1[i], hi, lo); r.h1[i] = hi; r.lo1[i] = lo;
-        split((rb[2] + alpha * rb[5]) - r.X2[i], hi, lo); r.h2[i] = hi; r.lo2[i] = lo;
+        const float* rb = r.ramp + 12 * (i - NF);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          float s, e;
+          two_sum(rb[k], alpha * rb[6 + k], s, e);
+          r.hi(k, i) = s;
+          r.lo(k, i) = e + rb[3 + k];
+        }
       }
     }
     __syncthreads();
     const bool dt_step = (step % kUpdateFreq) == 0;
-    const double lmin = fiber_pass_mixed(r, d, L, dt_step);
     if (dt_step) {
-      dt_crit = block_min<kThreadsMixed>(lmin, red) / d.sound_speed;
+      double lm = DBL_MAX;
+      for (int e = tid; e < E; e += kThreadsMixed) {
+        fiber_force(r, e);
+        lm = fmin(lm, length64(r, b.X, e));
+      }
+      dt_crit = block_min<kThreadsMixed>(lm, red) / d.sound_speed;
+      h_cur = static_cast<float>(d.crit * dt_crit * 0.5);
     } else {
+      int e = tid;
+      for (; e + kThreadsMixed < E; e += 2 * kThreadsMixed) {
+        fiber_force(r, e);
+        fiber_force(r, e + kThreadsMixed);
+      }
+      if (e < E) fiber_force(r, e);
       __syncthreads();
     }
     h_prev = h;
@@ -331,27 +413,33 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
 
   // ---- finalize: FP64 positions, boundary f_int, stress ---------------------
   for (int i = tid; i < N; i += kThreadsMixed) {
-    const double X0 = r.X0[i], X1 = r.X1[i], X2 = r.X2[i];
-    const double x0 = X0 + (static_cast<double>(r.h0[i]) + r.lo0[i]);
-    const double x1 = X1 + (static_cast<double>(r.h1[i]) + r.lo1[i]);
-    const double x2 = X2 + (static_cast<double>(r.h2[i]) + r.lo2[i]);
-    r.x0[i] = x0; r.x1[i] = x1; r.x2[i] = x2;
-    if (a.update_coords) {
-      r.u0[i] = x0 - X0; r.u1[i] = x1 - X1; r.u2[i] = x2 - X2;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double Xk = b.X[k * nt + no + i];
+      const double xk = Xk + (static_cast<double>(r.hi(k, i)) + r.lo(k, i));
+      b.x[k * nt + no + i] = xk;
+      if (a.update_coords) b.u[k * nt + no + i] = xk - Xk;
     }
     if (i >= NF) {
       float a0, a1, a2;
-      gather_f32(r, i, a0, a1, a2);
-      r.fi0[i] = a0; r.fi1[i] = a1; r.fi2[i] = a2;
+      gather(r, i, a0, a1, a2);
+      b.fint[no + i] = a0;
+      b.fint[nt + no + i] = a1;
+      b.fint[2 * nt + no + i] = a2;
     }
   }
   __syncthreads();
   if (tid < 6) {
     double s = 0.0;
     const int k = tid;
-    for (int i = NF; i < N; ++i) {
-      const double f1 = r.fi0[i], f2 = r.fi1[i], f3 = r.fi2[i];
-      const double crd1 = r.x0[i], crd2 = r.x1[i], crd3 = r.x2[i];
+    const int32_t* bo = b.bnd + d.bnd_off;
+    const double* x0 = b.x + no;
+    const double* x1 = b.x + nt + no;
+    const double* x2 = b.x + 2 * nt + no;
+    for (int q = 0; q < N - NF; ++q) {
+      const int i = bo[q];
+      const double f1 = b.fint[no + i], f2 = b.fint[nt + no + i], f3 = b.fint[2 * nt + no + i];
+      const double crd1 = x0[i], crd2 = x1[i], crd3 = x2[i];
       double t;
       switch (k) {
         case 0: t = crd1 * f1; break;
@@ -377,9 +465,9 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kThreadsMixed) relax_mixed_kernel(const DevBatch b,
-                                                                    const MixedState ms,
-                                                                    const RunArgs a) {
+__global__ void __launch_bounds__(kThreadsMixed, 1)
+relax_mixed_kernel(const DevBatch b, const MixedState ms, const RunArgs a, int smem_floats) {
+  extern __shared__ float smem[];
   __shared__ double red[kThreadsMixed / 32 + 1];
   __shared__ int s_rve;
   for (;;) {
@@ -391,7 +479,7 @@ __global__ void __launch_bounds__(kThreadsMixed) relax_mixed_kernel(const DevBat
     const int rve = s_rve;
     __syncthreads();
     if (rve < 0) break;
-    solve_rve_mixed(b, ms, a, rve, red);
+    solve_rve_mixed(b, ms, a, rve, red, smem, smem_floats);
   }
 }
 
@@ -406,7 +494,9 @@ MixedState* mixed_new() { return new MixedState(); }
 
 void mixed_destroy(MixedState* ms) {
   if (!ms) return;
-  for (float* p : {ms->u_hi, ms->u_lo, ms->v, ms->minv, ms->m32, ms->dX, ms->rl0, ms->nrm})
+  for (void* p : {static_cast<void*>(ms->u_hi), static_cast<void*>(ms->u_lo),
+                  static_cast<void*>(ms->v), static_cast<void*>(ms->mass),
+                  static_cast<void*>(ms->fcon), static_cast<void*>(ms->nrm)})
     if (p) cudaFree(p);
   delete ms;
 }
@@ -417,19 +507,15 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
   const size_t nt = static_cast<size_t>(b.nt), et = static_cast<size_t>(b.et);
   if ((e = alloc(&ms.u_hi, 3 * nt)) != cudaSuccess) return e;
   if ((e = alloc(&ms.u_lo, 3 * nt)) != cudaSuccess) return e;
-  if ((e = alloc(&ms.v, 3 * nt)) != cudaSuccess) return e;
-  if ((e = alloc(&ms.minv, nt)) != cudaSuccess) return e;
-  if ((e = alloc(&ms.m32, nt)) != cudaSuccess) return e;
-  if ((e = alloc(&ms.dX, 3 * et)) != cudaSuccess) return e;
-  if ((e = alloc(&ms.rl0, et)) != cudaSuccess) return e;
-  if ((e = alloc(&ms.nrm, 3 * et)) != cudaSuccess) return e;
+  if ((e = alloc(&ms.v, nt)) != cudaSuccess) return e;
+  if ((e = alloc(&ms.mass, nt)) != cudaSuccess) return e;
+  if ((e = alloc(&ms.fcon, et)) != cudaSuccess) return e;
+  if ((e = alloc(&ms.nrm, et)) != cudaSuccess) return e;
   ms.sms = sms;
-  int occ = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, relax_mixed_kernel, kThreadsMixed, 0) !=
-          cudaSuccess ||
-      occ < 1)
-    occ = 1;
-  ms.occ = occ;
+  ms.smem_bytes = kSmemBytesMixed;
+  if ((e = cudaFuncSetAttribute(relax_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                kSmemBytesMixed)) != cudaSuccess)
+    return e;
   const int64_t n = std::max<int64_t>(b.nt, 1);
   mixed_prepare_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(b, ms);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -443,8 +529,9 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
 
 cudaError_t run_mixed(MixedState& ms, const DevBatch& b, const RunArgs& a, cudaStream_t s,
                       int* launches) {
-  const int grid = std::min(b.n_rve, ms.sms * ms.occ);
-  relax_mixed_kernel<<<grid, kThreadsMixed, 0, s>>>(b, ms, a);
+  const int grid = std::min(b.n_rve, ms.sms);
+  relax_mixed_kernel<<<grid, kThreadsMixed, ms.smem_bytes, s>>>(b, ms, a,
+                                                               ms.smem_bytes / sizeof(float));
   *launches = 1;
   return cudaGetLastError();
 }
