@@ -232,6 +232,69 @@ mfg_status mfg_batch_run_device_noalloc(mfg_batch* batch, const double* F_dev, i
                                         double* sigma_dev, int32_t update_coords,
                                         mfg_rve_status* status_dev, void* stream);
 
+/* ---- serving --------------------------------------------------------- */
+/* Replaces the microscale service loop of the multiscale coupling
+ * (MultiscaleRVEAnalysis::run, src/mumfim/microscale/MultiscaleRVEAnalysis.cc:197-305):
+ * instead of one blocking batch per macro iteration, integration points
+ * submit deformation-gradient increments as they arrive and collect stresses
+ * as they complete. Every registered RVE keeps its state on the device
+ * between requests. A persistent kernel (one CTA per SM) claims requests from
+ * a ring in host-mapped memory and solves each RVE as soon as a CTA frees up,
+ * so requests that arrive while others are on the GPU join the running work
+ * (continuous batching). Each solve is the same deterministic per-RVE
+ * computation as mfg_batch_run(), so a result does not depend on what else is
+ * in flight. Requests for an RVE that is already in flight wait on the host
+ * and go out in submission order. */
+typedef struct mfg_server mfg_server;
+
+typedef struct mfg_server_options {
+  int32_t precision;        /* mfg_precision (MFG_PREC_MIXED is the served path) */
+  int32_t device;
+  int32_t capacity;         /* request ring entries; 0 = 65536 */
+  int32_t idle_timeout_us;  /* persistent kernel exits after this long without work; 0 = 20000 */
+  double hbm_budget_bytes;  /* admission cap on the device state of all RVEs; 0 = free HBM */
+  int32_t reserved[4];
+} mfg_server_options;
+
+/* One completed request. sigma maps onto micro_fo_result.data[0..5]
+ * (MultiscaleMicroFOParams.h:93-98). */
+typedef struct mfg_server_result {
+  int64_t ticket;
+  int32_t rve;
+  int32_t status;  /* MFG_OK, MFG_E_NOT_CONVERGED or MFG_E_NONFINITE */
+  int32_t steps;
+  int32_t pad_;
+  double residual;
+  double sigma[6];
+  double latency_s;  /* submit -> result seen by mfg_server_poll, host clock */
+  double device_s;   /* claim -> completion on the device */
+  int64_t t_claim_ns;  /* device %globaltimer when a CTA claimed the request */
+  int64_t t_done_ns;   /* device %globaltimer when its result was published */
+} mfg_server_result;
+
+void mfg_default_server_options(mfg_server_options* out);
+/* Registers n_rve RVEs (as mfg_batch_create) and starts serving. Returns
+ * MFG_E_BUSY when the RVEs' device state would exceed the HBM budget. */
+mfg_status mfg_server_create(const mfg_network* nets, const mfg_strategy* strategies,
+                             int32_t n_rve, const mfg_server_options* options, mfg_server** out);
+/* Queues one solve of `rve` with the row-major increment F (9 doubles,
+ * micro_fo_data.data). Non-blocking. MFG_E_BUSY when the ring is full. */
+mfg_status mfg_server_submit(mfg_server* server, int32_t rve, const double* F,
+                             int32_t update_coords, int64_t* ticket);
+/* Returns up to `capacity` completed requests, waiting up to timeout_ms for
+ * the first one. MFG_E_TIMEOUT when work is outstanding and none completed. */
+mfg_status mfg_server_poll(mfg_server* server, mfg_server_result* out, int32_t capacity,
+                           int32_t* n_out, int32_t timeout_ms);
+/* Requests submitted and not yet returned by mfg_server_poll. */
+int64_t mfg_server_outstanding(const mfg_server* server);
+/* Number of persistent-kernel launches so far. */
+int64_t mfg_server_launches(const mfg_server* server);
+/* The batch holding the RVE state, for state access while no request is
+ * outstanding (displacements, export/import, orientation tensors). */
+mfg_batch* mfg_server_batch(mfg_server* server);
+/* Stops the kernel (after the solves in flight), frees everything. */
+mfg_status mfg_server_destroy(mfg_server* server);
+
 /* ---- timing ----------------------------------------------------------- */
 /* Device time of the last run's relaxation kernel and of the whole run, in
  * milliseconds, from CUDA events recorded on the launching stream. Valid

@@ -92,3 +92,16 @@ class NetworkArray:
             self.strats[i] = mfg_strategy(float(s.visc_damp_coeff), float(s.crit_time_scale_factor),
                                           float(s.residual_tol), int(s.max_steps), int(s.mode))
         self.n = n
+
+
+class mfg_server_options(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("device", C.c_int32), ("capacity", C.c_int32),
+                ("idle_timeout_us", C.c_int32), ("hbm_budget_bytes", C.c_double),
+                ("reserved", C.c_int32 * 4)]
+
+
+SERVER_RESULT_DTYPE = np.dtype([("ticket", np.int64), ("rve", np.int32), ("status", np.int32),
+                                ("steps", np.int32), ("pad_", np.int32), ("residual", np.float64),
+                                ("sigma", np.float64, (6,)), ("latency_s", np.float64),
+                                ("device_s", np.float64), ("t_claim_ns", np.int64),
+                                ("t_done_ns", np.int64)])

@@ -853,3 +853,306 @@ mfg_status mfg_batch_last_timing(mfg_batch* b, float* relax_ms, float* run_ms) {
 int32_t mfg_batch_last_launches(const mfg_batch* b) { return b ? b->last_launches : 0; }
 
 }  // extern "C"
+
+// ============================================================================
+// Serving: continuous batching over a persistent kernel.
+// ============================================================================
+#include <chrono>
+#include <deque>
+
+namespace {
+
+double now_s() {
+  using namespace std::chrono;
+  return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct PendingReq {
+  int64_t ticket;
+  int32_t update;
+  double F[9];
+  double t_submit;
+};
+
+// Device footprint of a batch's state (FP64 arrays, CSR, and the mixed
+// working set when used), for admission against the HBM budget.
+double batch_bytes(int64_t nt, int64_t et, int64_t nbt, int64_t R, bool mixed) {
+  double b = nt * (5 * 3 * 8.0 + 8 + 4) + et * (8.0 + 8 + 24 + 8) + nbt * (48.0 + 4) + R * 200.0;
+  if (mixed) b += nt * (24.0 + 16 + 8) + et * (16.0 + 16);
+  return b;
+}
+
+}  // namespace
+
+struct mfg_server {
+  mfg_batch* batch = nullptr;
+  cudaStream_t stream = nullptr;
+  int64_t cap = 0;
+  unsigned long long idle_ns = 0;
+  mfg::ServerReq* ring_h = nullptr;
+  volatile long long* tail_h = nullptr;
+  volatile int32_t* stop_h = nullptr;
+  mfg::ServerDone* done_h = nullptr;
+  unsigned long long* head_d = nullptr;
+  mfg::ServerArgs args{};
+  DevArray<double> sigma, res;
+  DevArray<int32_t> st, steps;
+  int64_t tail = 0;         // ring entries published
+  int64_t oldest = 0;       // oldest ring entry not yet returned
+  int64_t next_ticket = 0;
+  int64_t launches = 0;
+  std::vector<int64_t> slot_ticket;
+  std::vector<double> slot_submit;
+  std::vector<uint8_t> slot_returned;
+  std::vector<uint8_t> busy;
+  std::vector<std::deque<PendingReq>> held;
+  int64_t n_held = 0;
+  bool launched = false;
+
+  ~mfg_server() {
+    if (batch) cudaSetDevice(batch->device);
+    if (stop_h) *stop_h = 1;
+    if (stream) {
+      cudaStreamSynchronize(stream);
+      cudaStreamDestroy(stream);
+    }
+    if (ring_h) cudaFreeHost(ring_h);
+    if (tail_h) cudaFreeHost(const_cast<long long*>(tail_h));
+    if (stop_h) cudaFreeHost(const_cast<int32_t*>(stop_h));
+    if (done_h) cudaFreeHost(done_h);
+    if (head_d) cudaFree(head_d);
+    sigma.release();
+    res.release();
+    st.release();
+    steps.release();
+    mfg_batch_destroy(batch);
+  }
+};
+
+namespace {
+
+mfg_status server_ensure_running(mfg_server* sv) {
+  if (sv->launched) {
+    cudaError_t q = cudaStreamQuery(sv->stream);
+    if (q == cudaErrorNotReady) return MFG_OK;
+    if (q != cudaSuccess)
+      return fail(MFG_E_CUDA, "serving kernel failed: %s", cudaGetErrorString(q));
+  }
+  cudaError_t e = sv->batch->precision == MFG_PREC_MIXED
+                      ? mfg::launch_server_mixed(*sv->batch->mixed, sv->batch->dev, sv->args,
+                                                 sv->stream)
+                      : mfg::launch_server_f64(sv->batch->dev, sv->args,
+                                               sv->batch->sms * mfg::relax_f64_max_blocks_per_sm(0),
+                                               sv->stream);
+  if (e != cudaSuccess) return fail(MFG_E_CUDA, "serving launch failed: %s", cudaGetErrorString(e));
+  sv->launched = true;
+  sv->launches++;
+  return MFG_OK;
+}
+
+// Writes one request into the ring and publishes it (release: entry, then tail).
+void server_publish(mfg_server* sv, int32_t rve, const PendingReq& p) {
+  const int64_t idx = sv->tail;
+  mfg::ServerReq& q = sv->ring_h[idx % sv->cap];
+  q.rve = rve;
+  q.update_coords = p.update;
+  q.ticket = p.ticket;
+  for (int k = 0; k < 9; ++k) q.F[k] = p.F[k];
+  sv->slot_ticket[idx % sv->cap] = p.ticket;
+  sv->slot_submit[idx % sv->cap] = p.t_submit;
+  sv->slot_returned[idx % sv->cap] = 0;
+  std::atomic_thread_fence(std::memory_order_seq_cst);
+  sv->tail = idx + 1;
+  *sv->tail_h = sv->tail;
+  std::atomic_thread_fence(std::memory_order_seq_cst);
+  sv->busy[rve] = 1;
+}
+
+}  // namespace
+
+extern "C" {
+
+void mfg_default_server_options(mfg_server_options* out) {
+  if (!out) return;
+  std::memset(out, 0, sizeof(*out));
+  out->precision = MFG_PREC_MIXED;
+}
+
+mfg_status mfg_server_create(const mfg_network* nets, const mfg_strategy* strategies,
+                             int32_t n_rve, const mfg_server_options* options, mfg_server** out) {
+  g_last_error.clear();
+  if (!out) return fail(MFG_E_INVALID, "out is NULL");
+  *out = nullptr;
+  mfg_server_options opt;
+  mfg_default_server_options(&opt);
+  if (options) opt = *options;
+  if (opt.capacity < 0 || opt.idle_timeout_us < 0 || !(opt.hbm_budget_bytes >= 0))
+    return fail(MFG_E_INVALID, "negative server option");
+  mfg_options bo;
+  mfg_default_options(&bo);
+  bo.precision = opt.precision;
+  bo.device = opt.device;
+  // admission: the device state of every registered RVE must fit the budget
+  if (nets && n_rve > 0) {
+    int64_t nt = 0, et = 0;
+    for (int r = 0; r < n_rve; ++r) {
+      nt += std::max(nets[r].n_nodes, 0);
+      et += std::max(nets[r].n_fibers, 0);
+    }
+    const double need = batch_bytes(nt, et, nt / 8, n_rve, opt.precision == MFG_PREC_MIXED);
+    double budget = opt.hbm_budget_bytes;
+    if (budget <= 0) {
+      size_t fr = 0, tot = 0;
+      if (cudaSetDevice(opt.device) == cudaSuccess && cudaMemGetInfo(&fr, &tot) == cudaSuccess)
+        budget = 0.9 * static_cast<double>(fr);
+    }
+    if (budget > 0 && need > budget)
+      return fail(MFG_E_BUSY, "admission refused: %.3g bytes of RVE state exceed the %.3g-byte "
+                  "HBM budget", need, budget);
+  }
+  mfg_batch* b = nullptr;
+  mfg_status st = mfg_batch_create(nets, strategies, n_rve, &bo, &b);
+  if (st != MFG_OK) return st;
+  std::unique_ptr<mfg_server> sv(new mfg_server());
+  sv->batch = b;
+  sv->cap = opt.capacity > 0 ? opt.capacity : 65536;
+  sv->idle_ns = 1000ULL * static_cast<unsigned long long>(opt.idle_timeout_us > 0 ? opt.idle_timeout_us
+                                                                                   : 20000);
+  MFG_CUDA(cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking));
+  MFG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&sv->ring_h), sv->cap * sizeof(mfg::ServerReq),
+                         cudaHostAllocMapped));
+  MFG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&sv->done_h), sv->cap * sizeof(mfg::ServerDone),
+                         cudaHostAllocMapped));
+  long long* tail = nullptr;
+  int32_t* stop = nullptr;
+  MFG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&tail), 64, cudaHostAllocMapped));
+  MFG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&stop), 64, cudaHostAllocMapped));
+  sv->tail_h = tail;
+  sv->stop_h = stop;
+  *sv->tail_h = 0;
+  *sv->stop_h = 0;
+  std::memset(sv->done_h, 0, sv->cap * sizeof(mfg::ServerDone));
+  MFG_CUDA(cudaMalloc(reinterpret_cast<void**>(&sv->head_d), sizeof(unsigned long long)));
+  MFG_CUDA(cudaMemset(sv->head_d, 0, sizeof(unsigned long long)));
+  MFG_CUDA(sv->sigma.alloc(6 * static_cast<size_t>(n_rve)));
+  MFG_CUDA(sv->res.alloc(n_rve));
+  MFG_CUDA(sv->st.alloc(n_rve));
+  MFG_CUDA(sv->steps.alloc(n_rve));
+  mfg::ServerArgs& a = sv->args;
+  MFG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(const_cast<mfg::ServerReq**>(&a.ring)),
+                                    sv->ring_h, 0));
+  MFG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(const_cast<long long**>(&a.tail)),
+                                    tail, 0));
+  MFG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(const_cast<int32_t**>(&a.stop)), stop,
+                                    0));
+  MFG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&a.done), sv->done_h, 0));
+  a.head = sv->head_d;
+  a.cap = sv->cap;
+  a.idle_ns = sv->idle_ns;
+  a.sigma = sv->sigma.p;
+  a.st_status = sv->st.p;
+  a.st_steps = sv->steps.p;
+  a.st_residual = sv->res.p;
+  sv->slot_ticket.assign(sv->cap, -1);
+  sv->slot_submit.assign(sv->cap, 0.0);
+  sv->slot_returned.assign(sv->cap, 1);
+  sv->busy.assign(n_rve, 0);
+  sv->held.resize(n_rve);
+  MFG_CUDA(cudaDeviceSynchronize());
+  *out = sv.release();
+  return MFG_OK;
+}
+
+mfg_status mfg_server_submit(mfg_server* sv, int32_t rve, const double* F, int32_t update_coords,
+                             int64_t* ticket) {
+  g_last_error.clear();
+  if (!sv || !F) return fail(MFG_E_INVALID, "NULL argument");
+  if (rve < 0 || rve >= sv->batch->R) return fail(MFG_E_INVALID, "rve %d out of range", rve);
+  for (int k = 0; k < 9; ++k)
+    if (!std::isfinite(F[k])) return fail(MFG_E_INVALID, "non-finite deformation gradient");
+  if (sv->tail - sv->oldest + sv->n_held >= sv->cap)
+    return fail(MFG_E_BUSY, "request ring full (%lld entries)", static_cast<long long>(sv->cap));
+  MFG_CUDA(cudaSetDevice(sv->batch->device));
+  PendingReq p;
+  p.ticket = sv->next_ticket++;
+  p.update = update_coords ? 1 : 0;
+  for (int k = 0; k < 9; ++k) p.F[k] = F[k];
+  p.t_submit = now_s();
+  if (ticket) *ticket = p.ticket;
+  if (sv->busy[rve]) {
+    sv->held[rve].push_back(p);
+    sv->n_held++;
+    return MFG_OK;
+  }
+  server_publish(sv, rve, p);
+  return server_ensure_running(sv);
+}
+
+mfg_status mfg_server_poll(mfg_server* sv, mfg_server_result* out, int32_t capacity,
+                           int32_t* n_out, int32_t timeout_ms) {
+  g_last_error.clear();
+  if (!sv || !n_out || (capacity > 0 && !out)) return fail(MFG_E_INVALID, "NULL argument");
+  *n_out = 0;
+  MFG_CUDA(cudaSetDevice(sv->batch->device));
+  const double t_end = now_s() + 1e-3 * std::max(timeout_ms, 0);
+  for (;;) {
+    int32_t n = 0;
+    for (int64_t idx = sv->oldest; idx < sv->tail && n < capacity; ++idx) {
+      const int64_t slot = idx % sv->cap;
+      if (sv->slot_returned[slot]) continue;
+      const mfg::ServerDone& d = sv->done_h[slot];
+      const long long flag = *reinterpret_cast<const volatile long long*>(&d.ticket_plus1);
+      if (flag != idx + 1) continue;
+      std::atomic_thread_fence(std::memory_order_acquire);
+      mfg_server_result& r = out[n++];
+      r.ticket = sv->slot_ticket[slot];
+      r.rve = d.rve;
+      r.status = d.status;
+      r.steps = d.steps;
+      r.pad_ = 0;
+      r.residual = d.residual;
+      for (int k = 0; k < 6; ++k) r.sigma[k] = d.sigma[k];
+      r.latency_s = now_s() - sv->slot_submit[slot];
+      r.device_s = 1e-9 * static_cast<double>(d.t_done_ns - d.t_claim_ns);
+      r.t_claim_ns = d.t_claim_ns;
+      r.t_done_ns = d.t_done_ns;
+      sv->slot_returned[slot] = 1;
+      sv->busy[d.rve] = 0;
+      if (!sv->held[d.rve].empty()) {
+        PendingReq p = sv->held[d.rve].front();
+        sv->held[d.rve].pop_front();
+        sv->n_held--;
+        server_publish(sv, d.rve, p);
+      }
+    }
+    while (sv->oldest < sv->tail && sv->slot_returned[sv->oldest % sv->cap]) sv->oldest++;
+    const bool outstanding = sv->tail > sv->oldest || sv->n_held > 0;
+    if (outstanding) {
+      mfg_status st = server_ensure_running(sv);
+      if (st != MFG_OK) return st;
+    }
+    if (n > 0) {
+      *n_out = n;
+      return MFG_OK;
+    }
+    if (!outstanding) return MFG_OK;
+    if (now_s() >= t_end)
+      return fail(MFG_E_TIMEOUT, "no request completed within %d ms", timeout_ms);
+    std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+}
+
+int64_t mfg_server_outstanding(const mfg_server* sv) {
+  return sv ? (sv->tail - sv->oldest + sv->n_held) : 0;
+}
+
+int64_t mfg_server_launches(const mfg_server* sv) { return sv ? sv->launches : 0; }
+
+mfg_batch* mfg_server_batch(mfg_server* sv) { return sv ? sv->batch : nullptr; }
+
+mfg_status mfg_server_destroy(mfg_server* sv) {
+  delete sv;
+  return MFG_OK;
+}
+
+}  // extern "C"

@@ -69,6 +69,36 @@ struct RunArgs {
   double* st_residual;  // device, n_rve
 };
 
+// Serving: request ring and completion records in host-mapped memory.
+struct ServerReq {
+  int32_t rve;
+  int32_t update_coords;
+  int64_t ticket;
+  double F[9];
+  double pad[1];
+};
+struct ServerDone {
+  int64_t ticket_plus1;  // written last: ticket + 1 once the record is valid
+  int32_t rve, status, steps, pad;
+  double residual;
+  double sigma[6];
+  int64_t t_claim_ns, t_done_ns;  // device %globaltimer
+};
+struct ServerArgs {
+  const ServerReq* ring;            // host-mapped, cap entries
+  const volatile long long* tail;   // host-mapped, requests published so far
+  const volatile int32_t* stop;     // host-mapped
+  unsigned long long* head;         // device, requests claimed so far
+  ServerDone* done;                 // host-mapped, cap entries
+  long long cap;
+  unsigned long long idle_ns;
+  double* sigma;                    // device per-RVE scratch, n_rve * 6
+  int32_t* st_status;
+  int32_t* st_steps;
+  double* st_residual;
+};
+cudaError_t launch_server_f64(const DevBatch& b, const ServerArgs& sa, int grid, cudaStream_t s);
+
 // Launchers (mfg_relax_f64.cu). Return cudaGetLastError() of the launch.
 cudaError_t launch_relax_f64(const DevBatch& b, const RunArgs& a, int threads, int grid,
                              cudaStream_t s);

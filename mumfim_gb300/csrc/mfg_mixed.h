@@ -22,6 +22,9 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
 cudaError_t run_mixed(MixedState& ms, const DevBatch& b, const RunArgs& a, cudaStream_t s,
                       int* launches);
 void mixed_destroy(MixedState* ms);
+// Persistent serving kernel on the mixed-precision solve (one CTA per SM).
+cudaError_t launch_server_mixed(MixedState& ms, const DevBatch& b, const ServerArgs& sa,
+                                cudaStream_t s);
 
 struct MixedStateDeleter {
   void operator()(MixedState* p) const { mixed_destroy(p); }

@@ -327,7 +327,18 @@ __global__ void __launch_bounds__(kThreadsF64) relax_f64_kernel(const DevBatch b
   }
 }
 
+__global__ void __launch_bounds__(kThreadsF64) server_f64_kernel(const DevBatch b,
+                                                                 const ServerArgs sa) {
+  __shared__ double red[kThreadsF64 / 32 + 1];
+  server_loop(sa, [&](const RunArgs& a, int rve) { solve_rve(b, a, rve, red); });
+}
+
 }  // namespace
+
+cudaError_t launch_server_f64(const DevBatch& b, const ServerArgs& sa, int grid, cudaStream_t s) {
+  server_f64_kernel<<<grid, kThreadsF64, 0, s>>>(b, sa);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_relax_f64(const DevBatch& b, const RunArgs& a, int threads, int grid,
                              cudaStream_t s) {

@@ -483,6 +483,15 @@ relax_mixed_kernel(const DevBatch b, const MixedState ms, const RunArgs a, int s
   }
 }
 
+__global__ void __launch_bounds__(kThreadsMixed, 1)
+server_mixed_kernel(const DevBatch b, const MixedState ms, const ServerArgs sa, int smem_floats) {
+  extern __shared__ float smem[];
+  __shared__ double red[kThreadsMixed / 32 + 1];
+  server_loop(sa, [&](const RunArgs& a, int rve) {
+    solve_rve_mixed(b, ms, a, rve, red, smem, smem_floats);
+  });
+}
+
 template <typename T>
 cudaError_t alloc(T** p, size_t n) {
   return cudaMalloc(reinterpret_cast<void**>(p), (n > 0 ? n : 1) * sizeof(T));
@@ -516,6 +525,9 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
   if ((e = cudaFuncSetAttribute(relax_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 kSmemBytesMixed)) != cudaSuccess)
     return e;
+  if ((e = cudaFuncSetAttribute(server_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                kSmemBytesMixed)) != cudaSuccess)
+    return e;
   const int64_t n = std::max<int64_t>(b.nt, 1);
   mixed_prepare_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(b, ms);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -524,6 +536,13 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
   dim3 grid(static_cast<unsigned>((max_e + 255) / 256),
             static_cast<unsigned>(std::min(b.n_rve, 65535)));
   mixed_prepare_fibers_kernel<<<grid, 256, 0, s>>>(b, ms);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_server_mixed(MixedState& ms, const DevBatch& b, const ServerArgs& sa,
+                                cudaStream_t s) {
+  server_mixed_kernel<<<ms.sms, kThreadsMixed, ms.smem_bytes, s>>>(b, ms, sa,
+                                                                   ms.smem_bytes / sizeof(float));
   return cudaGetLastError();
 }
 

@@ -1,0 +1,104 @@
+"""Continuous-batching server: requests join the running persistent kernel,
+results equal the batch API's, and a result does not depend on what else is
+in flight (deterministic per-RVE solves: bit-identical alone and in the mix)."""
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def W(lib_path):
+    from mumfim_gb300 import synthetic as S
+    return S.config2(n_rve=10, steps=800, n_min=400, n_max=3000)
+
+
+def _batch_sigma(m, w, precision, F=None, update=False):
+    g = m.BatchedFiberRVEAnalysisExplicit(w.networks, w.strategies, precision=precision)
+    sig = np.zeros((w.n_rve, 6))
+    g.run(w.F if F is None else F, sig, update_coords=update)
+    return sig
+
+
+@pytest.mark.parametrize("precision", ["mixed", "f64"])
+def test_alone_equals_in_the_mix_equals_batch(W, precision):
+    import mumfim_gb300 as m
+    from mumfim_gb300.serving import RVEServer
+    ref = _batch_sigma(m, W, precision)
+    with RVEServer(W.networks, W.strategies, precision=precision) as sv:
+        sv.submit(3, W.F[3], update_coords=False)
+        alone = sv.drain()
+        assert len(alone) == 1 and alone["rve"][0] == 3
+        for r in range(W.n_rve):
+            sv.submit(r, W.F[r], update_coords=False)
+        mix = sv.drain()
+    assert sorted(mix["rve"].tolist()) == list(range(W.n_rve))
+    np.testing.assert_array_equal(alone["sigma"][0], mix["sigma"][mix["rve"] == 3][0])
+    for rec in mix:
+        np.testing.assert_array_equal(rec["sigma"], ref[rec["rve"]])
+        assert rec["status"] == 0 and rec["steps"] == 800
+
+
+def test_requests_join_while_others_run(W):
+    """Submissions spread over time: later requests are claimed by CTAs
+    while earlier solves are still on the device (continuous batching)."""
+    import mumfim_gb300 as m
+    from mumfim_gb300.serving import RVEServer
+    ref = _batch_sigma(m, W, "mixed")
+    got = []
+    with RVEServer(W.networks, W.strategies, precision="mixed") as sv:
+        for r in range(W.n_rve):
+            sv.submit(r, W.F[r], update_coords=False)
+            time.sleep(0.002)
+            got.append(sv.poll(timeout_ms=0))
+        got.append(sv.drain())
+    res = np.concatenate(got)
+    assert len(res) == W.n_rve
+    for rec in res:
+        np.testing.assert_array_equal(rec["sigma"], ref[rec["rve"]])
+    # some request was claimed before an earlier-claimed one finished
+    order = np.argsort(res["t_claim_ns"])
+    claims, dones = res["t_claim_ns"][order], res["t_done_ns"][order]
+    assert any(claims[i + 1] < dones[i] for i in range(len(order) - 1))
+    assert (res["latency_s"] >= res["device_s"]).all()
+
+
+def test_same_rve_requests_run_in_submission_order(W):
+    """Two updating increments on one RVE: the second waits for the first and
+    the final state equals two sequential batch runs."""
+    import mumfim_gb300 as m
+    from mumfim_gb300.serving import RVEServer
+    F2 = np.eye(3) + 0.01 * np.array([[0, 1.0, 0], [0, 0, 0], [0, 0, -0.5]])
+    g = m.BatchedFiberRVEAnalysisExplicit(W.networks, W.strategies, precision="mixed")
+    s1, s2 = np.zeros((W.n_rve, 6)), np.zeros((W.n_rve, 6))
+    g.run(W.F, s1, update_coords=True)
+    g.run(np.repeat(F2[None], W.n_rve, 0), s2, update_coords=True)
+    with RVEServer(W.networks, W.strategies, precision="mixed") as sv:
+        t1 = sv.submit(5, W.F[5], update_coords=True)
+        t2 = sv.submit(5, F2, update_coords=True)
+        res = sv.drain()
+    res = res[np.argsort(res["ticket"])]
+    assert res["ticket"].tolist() == [t1, t2]
+    np.testing.assert_array_equal(res["sigma"][0], s1[5])
+    np.testing.assert_array_equal(res["sigma"][1], s2[5])
+
+
+def test_admission_ring_full_and_idle_relaunch(W):
+    import mumfim_gb300 as m
+    from mumfim_gb300.serving import RVEServer
+    with pytest.raises(m.MumfimGpuError) as ei:
+        RVEServer(W.networks, W.strategies, hbm_budget_bytes=1e5)
+    assert ei.value.status == 8 and "admission refused" in str(ei.value)
+    with RVEServer(W.networks, W.strategies, capacity=4, idle_timeout_us=1000) as sv:
+        for r in range(4):
+            sv.submit(r, W.F[r], update_coords=False)
+        with pytest.raises(m.MumfimGpuError) as ei:
+            sv.submit(4, W.F[4], update_coords=False)
+        assert ei.value.status == 8
+        assert len(sv.drain()) == 4
+        time.sleep(0.05)  # the kernel leaves after 1 ms without work
+        sv.submit(6, W.F[6], update_coords=False)
+        assert len(sv.drain()) == 1
+        assert sv.launches() >= 2
