@@ -1,12 +1,11 @@
 """Benchmark of the batched explicit fiber-network RVE solve.
 
-One bench step = one batched solve: every RVE of the workload relaxed for the
-configured number of explicit steps (RAMP protocol: the boundary follows F
-linearly over the solve), through the C ABI of libmumfim_gpu.so.
-
-Default workload (N = 1): config 1 -- 1024 RVEs x 4500 nodes, k = 4
-nearest-neighbour fibers (~11,100 fibers each), linear law, 5,000 steps,
-plain FP64 kernel. Metric: fiber-steps/s = sum over RVEs of fibers x steps,
+Default workload (N = 1): config 2, the uneven batch -- 4096 RVEs with node
+counts log-uniform in [500, 20000], kNN k in {3, 4, 5} (~52 M fibers), linear
+law, F = I + U(+-0.08), 5,000 explicit steps per solve (RAMP protocol: the
+boundary follows F linearly over the solve), mixed precision. One bench step
+is one batched solve of the whole workload through the C ABI of
+libmumfim_gpu.so. Metric: fiber-steps/s = sum over RVEs of fibers x steps,
 divided by wall time; RVE solves/s is reported beside it.
 
   value     inputs resident in HBM, K solves enqueued back to back on one
@@ -15,12 +14,20 @@ divided by wall time; RVE solves/s is reported beside it.
             step the host->device copy of the deformation gradients and the
             device->host copy of stresses and per-RVE status are inside the
             timed region
+  f64_same_batch  the plain FP64 kernel and the mixed kernel on the same
+            stratified subset of the batch (every 4th RVE): their throughput
+            ratio and the mixed stress error against FP64
+  served    a scaled config-4 stream through the continuous-batching server:
+            persistent RVEs (linear / nonlinear 50/50), load steps x Newton
+            iterations of increments I + U(+-0.005), Poisson arrivals at 80 %
+            of the measured capacity; throughput, p50/p99 latency, and the
+            stress error of a replayed subset against FP64
   roofline  the relaxation kernel's algorithmic bytes (per fiber-step
-            24 + 108 N/E bytes for FP64, counted from the workload) over its
-            CUDA-event duration, against the measured HBM copy bandwidth
+            20 B + 104 B per node for mixed, 24 B + 108 B per node for FP64)
+            over its CUDA-event duration, against the measured HBM bandwidth
   cpu_baseline  the CPU oracle (a restatement of the reference's batched
-            path: the reference itself cannot be built without Kokkos, PUMI,
-            AMSI and MPI) on the host's cores, on a bounded subset of RVEs
+            path: the reference itself needs Kokkos, PUMI, AMSI and MPI and
+            cannot be built) on all host cores, on the first RVEs of the batch
 
 ``--impl reference`` times only that CPU restatement on the same workload.
 Multi-GPU (torchrun): RVEs are independent; every rank solves its own batch
@@ -96,6 +103,7 @@ class ClockSampler:
         os.remove(self.path)
         if not rows:
             return None
+
         def num(x):
             try:
                 return float(x)
@@ -124,7 +132,8 @@ def build_workload(config: int, rank: int, n_rve: int | None, solve_steps: int |
     elif config == 2:
         n = n_rve or 4096
         w = S.config2(n_rve=n, first=rank * n, **kw)
-        desc = f"config2: {n} RVEs, nodes log-uniform [500,20000], k in {{3,4,5}}, {w.steps} ramp steps"
+        desc = (f"config2: {n} RVEs, nodes log-uniform [500,20000], k in {{3,4,5}}, linear law, "
+                f"F = I + U(+-0.08), {w.steps} ramp steps")
     elif config == 3:
         n = n_rve or 2048
         w = S.config3(n_rve=n, first=rank * n, **kw)
@@ -143,6 +152,11 @@ def algorithmic_bytes(w, precision: str) -> float:
     return float(w.steps) * (bf * w.total_fibers + bn * w.total_nodes)
 
 
+def rel_err(a, b):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
 def cpu_baseline(w, sample_rves: int, threads: int):
     from oracle import pyoracle
     sub = w.subset(range(min(sample_rves, w.n_rve)))
@@ -152,8 +166,9 @@ def cpu_baseline(w, sample_rves: int, threads: int):
     dt = time.perf_counter() - t0
     fs = sub.total_fibers * sub.steps
     return {"value": fs / dt, "unit": "fiber-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{sub.n_rve} RVEs of the workload x {sub.steps} steps "
-                      f"({fs:.3g} fiber-steps, {dt:.1f} s, oracle built -O2 -ffp-contract=off)",
+            "sample": f"first {sub.n_rve} RVEs of the workload x {sub.steps} steps "
+                      f"({fs:.3g} fiber-steps, {dt:.1f} s; oracle = C++ restatement of the "
+                      f"reference's batched path, -O2 -ffp-contract=off, one RVE per thread)",
             "rve_solves_per_s": sub.n_rve / dt}
 
 
@@ -180,15 +195,108 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": "fiber-steps/s", "value": value, "unit": "fiber-steps/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * tot / len(times), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded kNN networks)",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded kNN fiber networks)",
         "config": {"workload": desc, "sample_rves": sub.n_rve, "precision": "f64"},
         "cpu_baseline": {"value": value, "unit": "fiber-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{sub.n_rve} RVEs x {sub.steps} steps per step"},
+                         "sample": f"first {sub.n_rve} RVEs x {sub.steps} steps per step"},
         "e2e": {"value": value, "unit": "fiber-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "rve_solves_per_s": sub.n_rve * len(times) / tot,
     }
     print(json.dumps(line), flush=True)
+
+
+def f64_same_batch(m, w, every: int):
+    """Plain FP64 and mixed kernels on the same stratified subset."""
+    sub = w.subset(range(0, w.n_rve, every))
+    out = {}
+    sig = {}
+    for prec in ("f64", "mixed"):
+        g = m.BatchedFiberRVEAnalysisExplicit(sub.networks, sub.strategies, precision=prec)
+        s = np.zeros((sub.n_rve, 6))
+        g.run(sub.F, s, update_coords=False)  # warm
+        g.run(sub.F, s, update_coords=False)
+        relax_ms, _ = g.last_timing()
+        out[prec] = sub.total_fibers * sub.steps / (relax_ms * 1e-3)
+        sig[prec] = s.copy()
+        g.close()
+    return {"subset": f"every {every}th RVE ({sub.n_rve} RVEs, {sub.total_fibers} fibers)",
+            "f64_fiber_steps_per_s": out["f64"], "mixed_fiber_steps_per_s": out["mixed"],
+            "mixed_over_f64": out["mixed"] / out["f64"],
+            "sigma_rel_err_mixed_vs_f64": rel_err(sig["mixed"], sig["f64"])}
+
+
+def served(m, n_points: int, load_steps: int, iters: int, steps: int, capacity_fs: float,
+           check: int):
+    """Scaled config-4 stream through the continuous-batching server."""
+    from mumfim_gb300 import synthetic as S
+    from mumfim_gb300.serving import RVEServer
+    w = S.config4(n_points=n_points, steps=steps)
+    fib = np.array([n.n_fibers for n in w.networks], dtype=np.float64)
+    rate = 0.8 * capacity_fs / (fib.mean() * steps)  # requests per second
+    lat, dev = [], []
+    hist = {}  # point -> list of sigma per request (checked subset)
+    t_start = None
+    n_done = 0
+    with RVEServer(w.networks, w.strategies, precision="mixed") as sv:
+        for ls in range(load_steps):
+            for it in range(iters):
+                arrivals = S.poisson_arrivals(1000 * ls + it, n_points, rate)
+                order = np.argsort(S.uniform(7 + 1000 * ls + it, n_points))
+                t0 = time.perf_counter()
+                if t_start is None:
+                    t_start = t0
+                incs = [S.config4_increment(p, ls, it) for p in range(n_points)]
+                k = 0
+                pending = 0
+                while k < n_points or pending > 0:
+                    now = time.perf_counter() - t0
+                    while k < n_points and arrivals[k] <= now:
+                        p = int(order[k])
+                        sv.submit(p, incs[p], update_coords=True)
+                        k += 1
+                        pending += 1
+                    res = sv.poll(timeout_ms=0 if k < n_points else 50)
+                    pending -= len(res)
+                    n_done += len(res)
+                    lat.extend(res["latency_s"].tolist())
+                    dev.extend(res["device_s"].tolist())
+                    for rec in res:
+                        if rec["rve"] < check:
+                            hist.setdefault(int(rec["rve"]), []).append(rec["sigma"].copy())
+                    if k < n_points:
+                        time.sleep(min(max(arrivals[k] - (time.perf_counter() - t0), 0), 0.0005))
+        wall = time.perf_counter() - t_start
+        launches = sv.launches()
+    # replay the checked points on the plain FP64 kernel
+    sub = w.subset(range(check))
+    g = m.BatchedFiberRVEAnalysisExplicit(sub.networks, sub.strategies, precision="f64")
+    errs = []
+    for ls in range(load_steps):
+        for it in range(iters):
+            F = np.stack([S.config4_increment(p, ls, it) for p in range(check)])
+            s = np.zeros((check, 6))
+            g.run(F, s, update_coords=True)
+            j = ls * iters + it
+            got = np.stack([hist[p][j] for p in range(check)])
+            errs.append(rel_err(got, s))
+    g.close()
+    total_fs = float(fib.sum()) * steps * load_steps * iters
+    lat = np.array(lat)
+    return {
+        "workload": (f"config4 scaled: {n_points} persistent RVEs (of 20,000), nodes log-uniform "
+                     f"[500,20000], linear/nonlinear 50/50, {load_steps} load steps x {iters} Newton "
+                     f"iterations, increments I + U(+-0.005), {steps} ramp steps per request, "
+                     f"Poisson arrivals at {rate:.0f}/s (80 % of measured capacity)"),
+        "requests": int(n_done), "wall_s": wall,
+        "fiber_steps_per_s": total_fs / wall, "rve_solves_per_s": n_done / wall,
+        "latency_p50_ms": float(np.percentile(lat, 50) * 1e3),
+        "latency_p99_ms": float(np.percentile(lat, 99) * 1e3),
+        "device_p50_ms": float(np.percentile(dev, 50) * 1e3),
+        "kernel_launches": int(launches),
+        "sigma_rel_err_vs_f64": float(max(errs)),
+        "checked_points": check,
+    }
 
 
 def main():
@@ -197,13 +305,18 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", type=int, default=1)
+    ap.add_argument("--config", type=int, default=2)
     ap.add_argument("--n-rve", type=int, default=None)
-    ap.add_argument("--precision", default="f64", choices=["f64", "mixed"])
-    ap.add_argument("--cpu-sample-rves", type=int, default=48)
+    ap.add_argument("--precision", default="mixed", choices=["f64", "mixed"])
+    ap.add_argument("--cpu-sample-rves", type=int, default=64)
     ap.add_argument("--solve-steps", type=int, default=None,
                     help="override the explicit steps per solve (small profiling cases)")
+    ap.add_argument("--f64-every", type=int, default=4)
+    ap.add_argument("--serve-points", type=int, default=2048)
+    ap.add_argument("--serve-steps", type=int, default=500)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the FP64 side-by-side and the served stream")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
@@ -268,7 +381,6 @@ def main():
         ev[k + 1].record(stream)
     ev[-1].synchronize()
     barrier()
-    clk = clocks.stop()
     step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
     t_ms = sum(step_ms)
     launches_per_step = gpu.last_launches()
@@ -282,20 +394,20 @@ def main():
     # ---- e2e: host buffers through mfg_batch_run -----------------------------
     F_host = torch.from_numpy(np.ascontiguousarray(w.F.reshape(R, 3, 3))).pin_memory().numpy()
     sig_host = torch.zeros((R, 6), dtype=torch.float64).pin_memory().numpy()
-    for _ in range(args.warmup):
-        gpu.run(F_host, sig_host, update_coords=False)
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         gpu.run(F_host, sig_host, update_coords=False)
     barrier()
     e2e_s = time.perf_counter() - t0
+    clk = clocks.stop()
     if dist:
         t = torch.tensor([e2e_s], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e = world * fiber_steps * args.steps / e2e_s
     ok_frac = float(np.mean(gpu.last_status["status"] == 0))
+    gpu.close()
 
     # ---- roofline of the relaxation kernel -----------------------------------
     peak, peak_kind = _peaks()
@@ -325,18 +437,20 @@ def main():
         "gpu_launches": int(launches_per_step * args.steps),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "peak_source": f"{peak_kind} hbm_gbs",
-                     "kernel": "relax_f64_kernel" if args.precision == "f64" else "relax_mixed",
+                     "peak_source": f"{peak_kind} hbm_gbs (burst)",
+                     "kernel": "relax_f64_kernel" if args.precision == "f64" else "relax_mixed_kernel",
                      "kernel_ms": relax_ms},
         "converged_or_completed_frac": ok_frac,
     }
     if clk:
         line["clocks"] = clk
+    if rank == 0 and world == 1 and not args.no_extras:
+        line["f64_same_batch"] = f64_same_batch(m, w, args.f64_every)
+        line["served"] = served(m, args.serve_points, 2, 3, args.serve_steps, value, 32)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, args.cpu_sample_rves, os.cpu_count() or 1)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    gpu.close()
     if dist:
         dist.barrier()
         dist.destroy_process_group()

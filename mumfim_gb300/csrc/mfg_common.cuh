@@ -64,6 +64,53 @@ __device__ __forceinline__ double jacobian(const double* dg) {
 #define MFG_SERVER_LOOP_CUH
 namespace mfg {
 
+// System-scope accesses to host-mapped memory: the host writes the request
+// ring, tail and stop flag and reads the completion records while the kernel
+// runs, so these go around the GPU caches (relaxed / release at .sys scope).
+__device__ __forceinline__ long long ld_sys(const volatile long long* p) {
+  long long v;
+  asm volatile("ld.relaxed.sys.global.s64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_sys(const volatile int* p) {
+  int v;
+  asm volatile("ld.relaxed.sys.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ double ld_sys(const volatile double* p) {
+  double v;
+  asm volatile("ld.relaxed.sys.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ long long ld_acquire_sys(const volatile long long* p) {
+  long long v;
+  asm volatile("ld.acquire.sys.global.s64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_sys(volatile long long* p, long long v) {
+  asm volatile("st.relaxed.sys.global.s64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void st_sys(volatile int* p, int v) {
+  asm volatile("st.relaxed.sys.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_sys(volatile double* p, double v) {
+  asm volatile("st.relaxed.sys.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+__device__ __forceinline__ void st_release_sys(volatile long long* p, long long v) {
+  asm volatile("st.release.sys.global.s64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ long long ld_gpu(const volatile long long* p) {
+  long long v;
+  asm volatile("ld.relaxed.gpu.global.s64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_gpu(const volatile int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
 __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -71,11 +118,15 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 // Persistent serving loop of one CTA: claim the next request from the ring,
-// solve its RVE with `solve`, publish the completion record, repeat. Every
-// wait is bounded: a CTA that finds no work for `idle_ns` (or after
-// kServerMaxPolls polls) leaves; the host relaunches the kernel while work is
-// pending. Requests and completions live in host-mapped memory; the claim
-// counter lives in device memory.
+// solve its RVE with `solve`, publish the completion record, repeat.
+// Shutdown is collective, so the kernel never thins out to a few CTAs: a CTA
+// may start closing only when every CTA of the grid is waiting and no
+// request has been claimed anywhere for `idle_ns`; closing sets a flag that
+// makes every CTA leave at its next poll, and the host relaunches the kernel
+// whenever work is pending after it ended. Every wait is bounded (the idle
+// timeout, and kServerMaxPolls polls per wait). Requests and completions live in host-mapped memory; the counters
+// the CTAs poll (published, claimed, stop) live in device memory, so idle
+// CTAs never hammer a host cache line the host is writing.
 constexpr long long kServerMaxPolls = 1LL << 26;
 
 template <typename Solve>
@@ -87,28 +138,39 @@ __device__ void server_loop(const ServerArgs& sa, Solve solve) {
     if (threadIdx.x == 0) {
       long long idx = -1;
       const unsigned long long t0 = global_ns();
+      atomicAdd(sa.idle_ctas, 1);
       for (long long polls = 0; polls < kServerMaxPolls; ++polls) {
-        if (*sa.stop) break;
+        if (ld_gpu(sa.stop) || ld_gpu(sa.closing)) break;
         const unsigned long long h = *reinterpret_cast<volatile unsigned long long*>(sa.head);
-        const long long t = *sa.tail;
+        const long long t = ld_gpu(sa.tail);
         if (static_cast<long long>(h) < t) {
           if (atomicCAS(sa.head, h, h + 1) == h) {
             idx = static_cast<long long>(h);
+            atomicMax(sa.last_claim, global_ns());
             break;
           }
           continue;
         }
-        if (global_ns() - t0 > sa.idle_ns) break;
-        __nanosleep(1000);
+        const unsigned long long now = global_ns();
+        const unsigned long long last =
+            *reinterpret_cast<volatile unsigned long long*>(sa.last_claim);
+        const unsigned long long since = last > t0 ? last : t0;
+        if (now > since && now - since > sa.idle_ns &&
+            ld_gpu(sa.idle_ctas) == static_cast<int>(gridDim.x)) {
+          atomicExch(sa.closing, 1);
+          break;
+        }
+        __nanosleep(2000);
       }
+      atomicSub(sa.idle_ctas, 1);
       __threadfence_system();  // order the ring entry after the tail we saw
       if (idx >= 0) {
         // The host may reuse this ring slot after `cap` requests: read it with
         // volatile loads (no stale L1 line) into shared memory.
         const volatile ServerReq* q = sa.ring + (idx % sa.cap);
-        s_req[0] = q->rve;
-        s_req[1] = q->update_coords;
-        for (int k = 0; k < 9; ++k) s_F[k] = q->F[k];
+        s_req[0] = ld_sys(&q->rve);
+        s_req[1] = ld_sys(&q->update_coords);
+        for (int k = 0; k < 9; ++k) s_F[k] = ld_sys(&q->F[k]);
       }
       s_idx = idx;
     }
@@ -130,17 +192,16 @@ __device__ void server_loop(const ServerArgs& sa, Solve solve) {
     solve(a, rve);  // ends with __syncthreads()
     if (threadIdx.x == 0) {
       __threadfence();
-      ServerDone* d = sa.done + (idx % sa.cap);
-      d->rve = rve;
-      d->status = sa.st_status[rve];
-      d->steps = sa.st_steps[rve];
-      d->residual = sa.st_residual[rve];
-      for (int k = 0; k < 6; ++k) d->sigma[k] = sa.sigma[6 * rve + k];
-      d->t_claim_ns = static_cast<long long>(t_claim);
-      d->t_done_ns = static_cast<long long>(global_ns());
+      volatile ServerDone* d = sa.done + (idx % sa.cap);
+      st_sys(&d->rve, rve);
+      st_sys(&d->status, sa.st_status[rve]);
+      st_sys(&d->steps, sa.st_steps[rve]);
+      st_sys(&d->residual, sa.st_residual[rve]);
+      for (int k = 0; k < 6; ++k) st_sys(&d->sigma[k], sa.sigma[6 * rve + k]);
+      st_sys(&d->t_claim_ns, static_cast<long long>(t_claim));
+      st_sys(&d->t_done_ns, static_cast<long long>(global_ns()));
       __threadfence_system();
-      *reinterpret_cast<volatile long long*>(&d->ticket_plus1) = idx + 1;
-      __threadfence_system();
+      st_release_sys(&d->ticket_plus1, idx + 1);
     }
     __syncthreads();
   }

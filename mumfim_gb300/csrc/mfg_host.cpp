@@ -886,14 +886,19 @@ double batch_bytes(int64_t nt, int64_t et, int64_t nbt, int64_t R, bool mixed) {
 
 struct mfg_server {
   mfg_batch* batch = nullptr;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;   // the persistent kernel
+  cudaStream_t ctrl = nullptr;     // small copies of the published count and stop flag
   int64_t cap = 0;
   unsigned long long idle_ns = 0;
   mfg::ServerReq* ring_h = nullptr;
-  volatile long long* tail_h = nullptr;
-  volatile int32_t* stop_h = nullptr;
+  long long* tail_stage = nullptr;  // pinned, one published count per ring slot
+  int32_t* stop_stage = nullptr;    // pinned
+  long long* tail_d = nullptr;
+  int32_t* stop_d = nullptr;
   mfg::ServerDone* done_h = nullptr;
   unsigned long long* head_d = nullptr;
+  unsigned long long* last_d = nullptr;
+  int* ctl_d = nullptr;  // [0] idle CTAs, [1] closing
   mfg::ServerArgs args{};
   DevArray<double> sigma, res;
   DevArray<int32_t> st, steps;
@@ -911,16 +916,25 @@ struct mfg_server {
 
   ~mfg_server() {
     if (batch) cudaSetDevice(batch->device);
-    if (stop_h) *stop_h = 1;
+    if (stop_d && stop_stage && ctrl) {
+      *stop_stage = 1;
+      cudaMemcpyAsync(stop_d, stop_stage, sizeof(int32_t), cudaMemcpyHostToDevice, ctrl);
+      cudaStreamSynchronize(ctrl);
+    }
     if (stream) {
       cudaStreamSynchronize(stream);
       cudaStreamDestroy(stream);
     }
+    if (ctrl) cudaStreamDestroy(ctrl);
     if (ring_h) cudaFreeHost(ring_h);
-    if (tail_h) cudaFreeHost(const_cast<long long*>(tail_h));
-    if (stop_h) cudaFreeHost(const_cast<int32_t*>(stop_h));
+    if (tail_stage) cudaFreeHost(tail_stage);
+    if (stop_stage) cudaFreeHost(stop_stage);
     if (done_h) cudaFreeHost(done_h);
+    if (tail_d) cudaFree(tail_d);
+    if (stop_d) cudaFree(stop_d);
     if (head_d) cudaFree(head_d);
+    if (last_d) cudaFree(last_d);
+    if (ctl_d) cudaFree(ctl_d);
     sigma.release();
     res.release();
     st.release();
@@ -938,6 +952,8 @@ mfg_status server_ensure_running(mfg_server* sv) {
     if (q != cudaSuccess)
       return fail(MFG_E_CUDA, "serving kernel failed: %s", cudaGetErrorString(q));
   }
+  // a fresh kernel starts with no CTA waiting and the closing flag down
+  MFG_CUDA(cudaMemsetAsync(sv->ctl_d, 0, 2 * sizeof(int), sv->stream));
   cudaError_t e = sv->batch->precision == MFG_PREC_MIXED
                       ? mfg::launch_server_mixed(*sv->batch->mixed, sv->batch->dev, sv->args,
                                                  sv->stream)
@@ -950,8 +966,10 @@ mfg_status server_ensure_running(mfg_server* sv) {
   return MFG_OK;
 }
 
-// Writes one request into the ring and publishes it (release: entry, then tail).
-void server_publish(mfg_server* sv, int32_t rve, const PendingReq& p) {
+// Writes one request into the ring and publishes it: the entry is stored
+// first, then the new published count is copied into device memory on the
+// control stream, where the CTAs poll it.
+mfg_status server_publish(mfg_server* sv, int32_t rve, const PendingReq& p) {
   const int64_t idx = sv->tail;
   mfg::ServerReq& q = sv->ring_h[idx % sv->cap];
   q.rve = rve;
@@ -963,9 +981,11 @@ void server_publish(mfg_server* sv, int32_t rve, const PendingReq& p) {
   sv->slot_returned[idx % sv->cap] = 0;
   std::atomic_thread_fence(std::memory_order_seq_cst);
   sv->tail = idx + 1;
-  *sv->tail_h = sv->tail;
-  std::atomic_thread_fence(std::memory_order_seq_cst);
+  sv->tail_stage[idx % sv->cap] = sv->tail;
   sv->busy[rve] = 1;
+  MFG_CUDA(cudaMemcpyAsync(sv->tail_d, &sv->tail_stage[idx % sv->cap], sizeof(long long),
+                           cudaMemcpyHostToDevice, sv->ctrl));
+  return MFG_OK;
 }
 
 }  // namespace
@@ -1019,21 +1039,26 @@ mfg_status mfg_server_create(const mfg_network* nets, const mfg_strategy* strate
   sv->idle_ns = 1000ULL * static_cast<unsigned long long>(opt.idle_timeout_us > 0 ? opt.idle_timeout_us
                                                                                    : 20000);
   MFG_CUDA(cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking));
+  MFG_CUDA(cudaStreamCreateWithFlags(&sv->ctrl, cudaStreamNonBlocking));
   MFG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&sv->ring_h), sv->cap * sizeof(mfg::ServerReq),
                          cudaHostAllocMapped));
   MFG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&sv->done_h), sv->cap * sizeof(mfg::ServerDone),
                          cudaHostAllocMapped));
-  long long* tail = nullptr;
-  int32_t* stop = nullptr;
-  MFG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&tail), 64, cudaHostAllocMapped));
-  MFG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&stop), 64, cudaHostAllocMapped));
-  sv->tail_h = tail;
-  sv->stop_h = stop;
-  *sv->tail_h = 0;
-  *sv->stop_h = 0;
+  MFG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&sv->tail_stage), sv->cap * sizeof(long long),
+                         cudaHostAllocDefault));
+  MFG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&sv->stop_stage), 64, cudaHostAllocDefault));
+  MFG_CUDA(cudaMalloc(reinterpret_cast<void**>(&sv->tail_d), sizeof(long long)));
+  MFG_CUDA(cudaMalloc(reinterpret_cast<void**>(&sv->stop_d), sizeof(int32_t)));
+  MFG_CUDA(cudaMemset(sv->tail_d, 0, sizeof(long long)));
+  MFG_CUDA(cudaMemset(sv->stop_d, 0, sizeof(int32_t)));
+  *sv->stop_stage = 0;
   std::memset(sv->done_h, 0, sv->cap * sizeof(mfg::ServerDone));
   MFG_CUDA(cudaMalloc(reinterpret_cast<void**>(&sv->head_d), sizeof(unsigned long long)));
   MFG_CUDA(cudaMemset(sv->head_d, 0, sizeof(unsigned long long)));
+  MFG_CUDA(cudaMalloc(reinterpret_cast<void**>(&sv->last_d), sizeof(unsigned long long)));
+  MFG_CUDA(cudaMemset(sv->last_d, 0, sizeof(unsigned long long)));
+  MFG_CUDA(cudaMalloc(reinterpret_cast<void**>(&sv->ctl_d), 2 * sizeof(int)));
+  MFG_CUDA(cudaMemset(sv->ctl_d, 0, 2 * sizeof(int)));
   MFG_CUDA(sv->sigma.alloc(6 * static_cast<size_t>(n_rve)));
   MFG_CUDA(sv->res.alloc(n_rve));
   MFG_CUDA(sv->st.alloc(n_rve));
@@ -1041,12 +1066,13 @@ mfg_status mfg_server_create(const mfg_network* nets, const mfg_strategy* strate
   mfg::ServerArgs& a = sv->args;
   MFG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(const_cast<mfg::ServerReq**>(&a.ring)),
                                     sv->ring_h, 0));
-  MFG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(const_cast<long long**>(&a.tail)),
-                                    tail, 0));
-  MFG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(const_cast<int32_t**>(&a.stop)), stop,
-                                    0));
+  a.tail = sv->tail_d;
+  a.stop = sv->stop_d;
   MFG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&a.done), sv->done_h, 0));
   a.head = sv->head_d;
+  a.last_claim = sv->last_d;
+  a.idle_ctas = sv->ctl_d;
+  a.closing = sv->ctl_d + 1;
   a.cap = sv->cap;
   a.idle_ns = sv->idle_ns;
   a.sigma = sv->sigma.p;
@@ -1084,7 +1110,8 @@ mfg_status mfg_server_submit(mfg_server* sv, int32_t rve, const double* F, int32
     sv->n_held++;
     return MFG_OK;
   }
-  server_publish(sv, rve, p);
+  mfg_status st = server_publish(sv, rve, p);
+  if (st != MFG_OK) return st;
   return server_ensure_running(sv);
 }
 
@@ -1122,7 +1149,8 @@ mfg_status mfg_server_poll(mfg_server* sv, mfg_server_result* out, int32_t capac
         PendingReq p = sv->held[d.rve].front();
         sv->held[d.rve].pop_front();
         sv->n_held--;
-        server_publish(sv, d.rve, p);
+        mfg_status st = server_publish(sv, d.rve, p);
+        if (st != MFG_OK) return st;
       }
     }
     while (sv->oldest < sv->tail && sv->slot_returned[sv->oldest % sv->cap]) sv->oldest++;

@@ -71,24 +71,27 @@ struct RunArgs {
 
 // Serving: request ring and completion records in host-mapped memory.
 struct ServerReq {
-  int32_t rve;
-  int32_t update_coords;
-  int64_t ticket;
+  int rve;
+  int update_coords;
+  long long ticket;
   double F[9];
   double pad[1];
 };
 struct ServerDone {
-  int64_t ticket_plus1;  // written last: ticket + 1 once the record is valid
-  int32_t rve, status, steps, pad;
+  long long ticket_plus1;  // written last: ticket + 1 once the record is valid
+  int rve, status, steps, pad;
   double residual;
   double sigma[6];
-  int64_t t_claim_ns, t_done_ns;  // device %globaltimer
+  long long t_claim_ns, t_done_ns;  // device %globaltimer
 };
 struct ServerArgs {
   const ServerReq* ring;            // host-mapped, cap entries
-  const volatile long long* tail;   // host-mapped, requests published so far
-  const volatile int32_t* stop;     // host-mapped
+  const volatile long long* tail;   // device: requests published so far (copied in by the host)
+  const volatile int32_t* stop;     // device: set by the host to end the kernel
   unsigned long long* head;         // device, requests claimed so far
+  unsigned long long* last_claim;   // device, %globaltimer of the latest claim by any CTA
+  int* idle_ctas;                   // device, CTAs currently waiting for work
+  int* closing;                     // device, set once the kernel is shutting down
   ServerDone* done;                 // host-mapped, cap entries
   long long cap;
   unsigned long long idle_ns;

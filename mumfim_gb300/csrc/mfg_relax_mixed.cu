@@ -43,7 +43,8 @@ struct MixedState {
   float* u_lo = nullptr;   // 3 * nt
   float4* v = nullptr;     // nt, velocity (w unused)
   float2* mass = nullptr;  // nt, (1 / m, m)
-  float4* fcon = nullptr;  // et, (X[n2] - X[n1], 1 / l0)
+  float4* fcon = nullptr;  // et, (X[n2] - X[n1], 1 / l0) rounded to FP32
+  float4* fclo = nullptr;  // et, remainders: the FP64 values minus fcon
   float4* nrm = nullptr;   // et, per-fiber force vectors (scratch; w unused)
   int sms = 1;
   int smem_bytes = 0;
@@ -69,12 +70,17 @@ __global__ void mixed_prepare_fibers_kernel(const DevBatch b, MixedState ms) {
     if (e >= d.n_fibers) continue;
     const int64_t fo = d.fiber_off + e, no = d.node_off;
     const int2 c = b.conn[fo];
-    float dx[3];
+    float dx[3], dxl[3];
     for (int k = 0; k < 3; ++k) {
       const double* X = b.X + k * b.nt + no;
-      dx[k] = static_cast<float>(X[c.y] - X[c.x]);
+      const double v = X[c.y] - X[c.x];
+      dx[k] = static_cast<float>(v);
+      dxl[k] = static_cast<float>(v - static_cast<double>(dx[k]));
     }
-    ms.fcon[fo] = make_float4(dx[0], dx[1], dx[2], static_cast<float>(1.0 / b.l0[fo]));
+    const double rl = 1.0 / b.l0[fo];
+    const float rh = static_cast<float>(rl);
+    ms.fcon[fo] = make_float4(dx[0], dx[1], dx[2], rh);
+    ms.fclo[fo] = make_float4(dxl[0], dxl[1], dxl[2], static_cast<float>(rl - static_cast<double>(rh)));
   }
 }
 
@@ -166,10 +172,11 @@ struct Rve {
   float4* v;            // node velocity (global)
   const float2* mass;   // (1 / m, m)
   const float4* fcon;   // (dX, 1 / l0)
+  const float4* fclo;   // their FP32 remainders
   const int2* conn;
   const int32_t* rowptr;
   const int32_t* inc;
-  float* ramp;          // per boundary node: u0_hi[3], u0_lo[3], d[3]
+  float* ramp;          // per boundary node: step increment d/n as (hi[3], lo[3])
   int64_t node_off, nt;
 };
 
@@ -190,37 +197,91 @@ __device__ __forceinline__ void gather(const Rve& r, int i, float& a0, float& a1
 #pragma unroll
   for (int j = 0; j < kGatherWidth; ++j)
     if (j < n) t[j] = r.n[code[j] >> 1];
+  // compensated (TwoSum) accumulation: the net force of a node is often a
+  // small difference of much larger fiber forces
+  float c0 = 0.f, c1 = 0.f, c2 = 0.f;
 #pragma unroll
   for (int j = 0; j < kGatherWidth; ++j) {
     if (j < n) {
       const float s = (code[j] & 1) ? 1.f : -1.f;
-      a0 = fmaf(s, t[j].x, a0);
-      a1 = fmaf(s, t[j].y, a1);
-      a2 = fmaf(s, t[j].z, a2);
+      float q, e;
+      two_sum(a0, s * t[j].x, q, e); a0 = q; c0 += e;
+      two_sum(a1, s * t[j].y, q, e); a1 = q; c1 += e;
+      two_sum(a2, s * t[j].z, q, e); a2 = q; c2 += e;
     }
   }
   for (int p = pb + kGatherWidth; p < pe; ++p) {
-    const int c = __ldg(r.inc + p);
-    const float4 tv = r.n[c >> 1];
-    const float s = (c & 1) ? 1.f : -1.f;
-    a0 = fmaf(s, tv.x, a0);
-    a1 = fmaf(s, tv.y, a1);
-    a2 = fmaf(s, tv.z, a2);
+    const int cd = __ldg(r.inc + p);
+    const float4 tv = r.n[cd >> 1];
+    const float s = (cd & 1) ? 1.f : -1.f;
+    float q, e;
+    two_sum(a0, s * tv.x, q, e); a0 = q; c0 += e;
+    two_sum(a1, s * tv.y, q, e); a1 = q; c1 += e;
+    two_sum(a2, s * tv.z, q, e); a2 = q; c2 += e;
   }
+  a0 += c0;
+  a1 += c1;
+  a2 += c2;
+}
+
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+  p = a * b;
+  e = fmaf(a, b, -p);
+}
+
+// Green-strain numerator dX.du + du.du/2 of one fiber, accurate to a few
+// FP32 ulps of ITS OWN value. A fiber that mostly rotates has
+// dX.du ~ -du.du/2, and plain FP32 leaves an error ~ulp(|dX||du|): in
+// sub-isostatic networks such rotation-dominated fibers carry the soft modes,
+// which amplify that error into the stress. Here du is kept as an unevaluated
+// sum dh + dl (TwoSum of the hi parts plus the lo parts), the leading products
+// are split exactly with FMA (TwoProd) and the terms are added with
+// compensated (TwoSum) summation.
+__device__ __forceinline__ float strain_numerator(const float* X, const float* Xl,
+                                                  const float* dh, const float* dl) {
+  float S = 0.f, C = 0.f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float p, ep, q, eq, s, es;
+    two_prod(X[k], dh[k], p, ep);
+    const float hk = 0.5f * dh[k];
+    two_prod(hk, dh[k], q, eq);
+    two_sum(S, p, s, es);
+    S = s;
+    C += es + ep;
+    two_sum(S, q, s, es);
+    S = s;
+    C += es + eq;
+    C = fmaf(X[k] + dh[k], dl[k], C);  // dX dl + dh dl (dl^2 is below FP32 resolution)
+    C = fmaf(Xl[k], dh[k], C);         // remainder of dX times du
+  }
+  return S + C;
 }
 
 __device__ __forceinline__ void fiber_force(const Rve& r, int e) {
   const int2 c = __ldg(r.conn + e);
-  const float du0 = (r.hi(0, c.y) - r.hi(0, c.x)) + (r.lo(0, c.y) - r.lo(0, c.x));
-  const float du1 = (r.hi(1, c.y) - r.hi(1, c.x)) + (r.lo(1, c.y) - r.lo(1, c.x));
-  const float du2 = (r.hi(2, c.y) - r.hi(2, c.x)) + (r.lo(2, c.y) - r.lo(2, c.x));
+  float dh[3], dl[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float d, ed;
+    two_sum(r.hi(k, c.y), -r.hi(k, c.x), d, ed);
+    dh[k] = d;
+    dl[k] = ed + (r.lo(k, c.y) - r.lo(k, c.x));
+  }
   const float4 fc = __ldg(r.fcon + e);
-  const float X0 = fc.x, X1 = fc.y, X2 = fc.z, rl0 = fc.w;
-  const float dxdu = fmaf(X0, du0, fmaf(X1, du1, X2 * du2));
-  const float dudu = fmaf(du0, du0, fmaf(du1, du1, du2 * du2));
-  const float g = fmaf(0.5f, dudu, dxdu) * (rl0 * rl0);
+  const float4 fl = __ldg(r.fclo + e);
+  const float X[3] = {fc.x, fc.y, fc.z};
+  const float Xl[3] = {fl.x, fl.y, fl.z};
+  // 1/l0^2 and 1/l0 from the (hi, lo) pair
+  float r2, e2;
+  two_prod(fc.w, fc.w, r2, e2);
+  r2 = r2 + fmaf(2.f * fc.w, fl.w, e2);
+  const float rl0 = fc.w + fl.w;
+  const float g = strain_numerator(X, Xl, dh, dl) * r2;
   const float t = tension_over_length(r.L, g, rl0);
-  r.n[e] = make_float4((X0 + du0) * t, (X1 + du1) * t, (X2 + du2) * t, 0.f);
+  r.n[e] = make_float4((X[0] + (dh[0] + (dl[0] + Xl[0]))) * t,
+                       (X[1] + (dh[1] + (dl[1] + Xl[1]))) * t,
+                       (X[2] + (dh[2] + (dl[2] + Xl[2]))) * t, 0.f);
 }
 
 // FP64 length of one fiber in the current configuration.
@@ -268,6 +329,7 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   r.v = ms.v + no;
   r.mass = ms.mass + no;
   r.fcon = ms.fcon + fo;
+  r.fclo = ms.fclo + fo;
   r.conn = b.conn + fo;
   r.rowptr = b.rowptr + d.row_off;
   r.inc = b.inc + d.inc_off;
@@ -305,14 +367,20 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
     }
     r.v[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (ramp && i >= NF) {
+      // The boundary moves by d/n per step, d = (F - I) x0. The increment is
+      // kept as an exact FP32 pair and accumulated without rounding into
+      // (hi, lo): recomputing u0 + alpha d in FP32 every step would jitter
+      // the boundary by ~ulp(d) per step, i.e. a large strain noise on the
+      // very short fibers that kNN networks attach to the boundary.
       float* rb = r.ramp + 12 * (i - NF);
+      const double inv_n = 1.0 / static_cast<double>(d.max_steps);
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        rb[k] = r.hi(k, i);
-        rb[3 + k] = r.lo(k, i);
-        rb[6 + k] = static_cast<float>((Fm[3 * k + 0] - (k == 0)) * xn[0] +
-                                       (Fm[3 * k + 1] - (k == 1)) * xn[1] +
-                                       (Fm[3 * k + 2] - (k == 2)) * xn[2]);
+        const double inc = ((Fm[3 * k + 0] - (k == 0)) * xn[0] + (Fm[3 * k + 1] - (k == 1)) * xn[1] +
+                            (Fm[3 * k + 2] - (k == 2)) * xn[2]) * inv_n;
+        const float ih = static_cast<float>(inc);
+        rb[k] = ih;
+        rb[3 + k] = static_cast<float>(inc - static_cast<double>(ih));
       }
     }
   }
@@ -326,7 +394,6 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
 
   const int cap = d.max_steps;
   const float c = static_cast<float>(d.c);
-  const float inv_steps = 1.f / static_cast<float>(d.max_steps);
   float h_cur = static_cast<float>(d.crit * dt_crit * 0.5);
   int step = 0;
   double residual = 10.0;
@@ -375,15 +442,14 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
       }
     }
     if (ramp) {
-      const float alpha = static_cast<float>(step + 1) * inv_steps;
       for (int i = NF + tid; i < N; i += kThreadsMixed) {
         const float* rb = r.ramp + 12 * (i - NF);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
           float s, e;
-          two_sum(rb[k], alpha * rb[6 + k], s, e);
+          two_sum(r.hi(k, i), rb[k], s, e);
           r.hi(k, i) = s;
-          r.lo(k, i) = e + rb[3 + k];
+          r.lo(k, i) = r.lo(k, i) + (e + rb[3 + k]);
         }
       }
     }
@@ -505,7 +571,8 @@ void mixed_destroy(MixedState* ms) {
   if (!ms) return;
   for (void* p : {static_cast<void*>(ms->u_hi), static_cast<void*>(ms->u_lo),
                   static_cast<void*>(ms->v), static_cast<void*>(ms->mass),
-                  static_cast<void*>(ms->fcon), static_cast<void*>(ms->nrm)})
+                  static_cast<void*>(ms->fcon), static_cast<void*>(ms->fclo),
+                  static_cast<void*>(ms->nrm)})
     if (p) cudaFree(p);
   delete ms;
 }
@@ -519,6 +586,7 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
   if ((e = alloc(&ms.v, nt)) != cudaSuccess) return e;
   if ((e = alloc(&ms.mass, nt)) != cudaSuccess) return e;
   if ((e = alloc(&ms.fcon, et)) != cudaSuccess) return e;
+  if ((e = alloc(&ms.fclo, et)) != cudaSuccess) return e;
   if ((e = alloc(&ms.nrm, et)) != cudaSuccess) return e;
   ms.sms = sms;
   ms.smem_bytes = kSmemBytesMixed;

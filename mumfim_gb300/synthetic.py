@@ -195,3 +195,41 @@ def config3(n_rve: int = 2048, steps: int = 20_000, first: int = 0,
     nets = [r[0] for r in res]
     F = np.stack([r[1] for r in res])
     return Workload("config3", nets, [SolutionStrategy.ramp(steps, 0.5) for _ in nets], F, steps)
+
+
+def config4(n_points: int = 20_000, steps: int = 500, first: int = 0,
+            n_min: int = 500, n_max: int = 20_000) -> Workload:
+    """Serving stream: one persistent RVE per integration point, nodes
+    log-uniform in [500, 20000], linear or exponential-toe law 50/50 with the
+    distributions of configs 2 and 3; each request relaxes `steps` RAMP
+    steps. F holds the identity; increments come from config4_increment()."""
+    def one(i):
+        r = first + i
+        u = uniform(param_seed(4, r) + 1, 8)
+        n = int(round(pexp(plog(n_min) + u[0] * (plog(n_max) - plog(n_min)))))
+        k = 3 + min(int(u[1] * 3), 2)
+        coords, conn = knn_network(n, k, geometry_seed(4, r))
+        if u[2] < 0.5:
+            rc = _linear_params(4, r)
+        else:
+            z = normal(param_seed(4, r), 1)
+            rc = Reaction(NONLINEAR, 1e-3, pexp(0.3 * z[0]), 1.0, 1.0 + 9.0 * u[3],
+                          1.02 + 0.13 * u[4])
+        return FiberNetwork(coords, conn, [rc])
+
+    nets = _parallel(one, n_points)
+    F = np.repeat(np.eye(3)[None], n_points, 0)
+    return Workload("config4", nets, [SolutionStrategy.ramp(steps, 0.5) for _ in nets], F, steps)
+
+
+def config4_increment(point: int, load_step: int, iteration: int) -> np.ndarray:
+    """Deformation-gradient increment of one request: I + U(+-0.005) entries."""
+    seed = param_seed(4, point) ^ (((load_step & 0xFFFF) << 16) | (iteration & 0xFFFF)) ^ 0xABCDEF
+    return np.eye(3) + (uniform(seed, 9) * 0.01 - 0.005).reshape(3, 3)
+
+
+def poisson_arrivals(seed: int, n: int, rate: float) -> np.ndarray:
+    """Arrival offsets (s) of a Poisson stream of n requests at `rate` per s."""
+    u = uniform(seed, n)
+    gaps = np.array([-plog(1.0 - x) for x in u]) / rate
+    return np.cumsum(gaps)

@@ -13,6 +13,7 @@
 // (TEAM_SIZE = 1) order for every team loop and atomic scatter.
 #include "mumfim_oracle.h"
 
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -279,6 +280,8 @@ void run_one(Rve& r, const double* F, double* sigma, bool update_coords, mfg_rve
     st->status = MFG_E_NONFINITE;
 }
 
+// Solves RVEs on n_threads host threads, one RVE per thread at a time, each
+// thread taking the next unsolved RVE (balances RVEs of uneven size).
 template <typename Fn>
 void parallel_over(int n, int n_threads, Fn fn) {
   if (n_threads <= 1 || n <= 1) {
@@ -286,13 +289,11 @@ void parallel_over(int n, int n_threads, Fn fn) {
     return;
   }
   if (n_threads > n) n_threads = n;
+  std::atomic<int> next{0};
   std::vector<std::thread> th;
   for (int t = 0; t < n_threads; ++t) {
-    th.emplace_back([=]() {
-      // static schedule: contiguous chunks
-      int lo = static_cast<int>(static_cast<long long>(n) * t / n_threads);
-      int hi = static_cast<int>(static_cast<long long>(n) * (t + 1) / n_threads);
-      for (int i = lo; i < hi; ++i) fn(i);
+    th.emplace_back([&]() {
+      for (int i = next++; i < n; i = next++) fn(i);
     });
   }
   for (auto& x : th) x.join();

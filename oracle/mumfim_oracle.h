@@ -26,8 +26,9 @@ typedef struct orc_batch orc_batch;
 
 orc_batch* orc_batch_create(const mfg_network* nets, const mfg_strategy* ss, int32_t n_rve);
 void orc_batch_destroy(orc_batch* b);
-/* n_threads > 1 solves RVEs concurrently (static partition over RVEs, one RVE
- * per thread at a time, as a Kokkos host build with TEAM_SIZE=1 does). */
+/* n_threads > 1 solves RVEs concurrently, one RVE per thread at a time (the
+ * structure of a Kokkos host build with TEAM_SIZE=1), each thread taking the
+ * next unsolved RVE. */
 int32_t orc_batch_run(orc_batch* b, const double* F, int32_t n_F, double* sigma,
                       int32_t update_coords, mfg_rve_status* status, int32_t n_threads);
 int32_t orc_batch_material_stiffness(orc_batch* b, double* C, int32_t n_threads);
