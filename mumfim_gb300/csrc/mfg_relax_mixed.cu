@@ -12,6 +12,10 @@
 //    precision at small strain (the length-ratio form 0.5(l^2/l0^2 - 1)
 //    cancels catastrophically in FP32). For the linear law
 //    T/l = lambda E A g / l = E A g / l0 needs neither sqrt nor division;
+//  - the RAMP boundary moves by an exact FP32 (hi, lo) per-step increment,
+//    accumulated with TwoSum: recomputing u0 + alpha d in FP32 every step
+//    jitters boundary nodes by ~ulp(d), which the very short fibers kNN
+//    networks attach to the boundary turn into large strain noise;
 //  - velocities, the damping force and both kicks are FP32;
 //  - FP64 is kept for the critical time step (FP64 lengths every 100 steps),
 //    the residual norm, and the stress homogenisation, exactly where the
@@ -44,7 +48,6 @@ struct MixedState {
   float4* v = nullptr;     // nt, velocity (w unused)
   float2* mass = nullptr;  // nt, (1 / m, m)
   float4* fcon = nullptr;  // et, (X[n2] - X[n1], 1 / l0) rounded to FP32
-  float4* fclo = nullptr;  // et, remainders: the FP64 values minus fcon
   float4* nrm = nullptr;   // et, per-fiber force vectors (scratch; w unused)
   int sms = 1;
   int smem_bytes = 0;
@@ -70,17 +73,12 @@ __global__ void mixed_prepare_fibers_kernel(const DevBatch b, MixedState ms) {
     if (e >= d.n_fibers) continue;
     const int64_t fo = d.fiber_off + e, no = d.node_off;
     const int2 c = b.conn[fo];
-    float dx[3], dxl[3];
+    float dx[3];
     for (int k = 0; k < 3; ++k) {
       const double* X = b.X + k * b.nt + no;
-      const double v = X[c.y] - X[c.x];
-      dx[k] = static_cast<float>(v);
-      dxl[k] = static_cast<float>(v - static_cast<double>(dx[k]));
+      dx[k] = static_cast<float>(X[c.y] - X[c.x]);
     }
-    const double rl = 1.0 / b.l0[fo];
-    const float rh = static_cast<float>(rl);
-    ms.fcon[fo] = make_float4(dx[0], dx[1], dx[2], rh);
-    ms.fclo[fo] = make_float4(dxl[0], dxl[1], dxl[2], static_cast<float>(rl - static_cast<double>(rh)));
+    ms.fcon[fo] = make_float4(dx[0], dx[1], dx[2], static_cast<float>(1.0 / b.l0[fo]));
   }
 }
 
@@ -157,11 +155,15 @@ __device__ __forceinline__ void split(double u, float& hi, float& lo) {
   lo = static_cast<float>(u - static_cast<double>(hi));
 }
 
-// A three-component float field: component k of node/fiber i at p[k*s + i].
+// A three-component float field: component k of node i at c[k][i].
 struct Field3 {
-  float* p;
-  int64_t s;
-  __device__ __forceinline__ float& operator()(int k, int i) const { return p[k * s + i]; }
+  float* c[3];
+  __device__ __forceinline__ void set(float* base, int64_t stride) {
+    c[0] = base;
+    c[1] = base + stride;
+    c[2] = base + 2 * stride;
+  }
+  __device__ __forceinline__ float& operator()(int k, int i) const { return c[k][i]; }
 };
 
 struct Rve {
@@ -172,7 +174,6 @@ struct Rve {
   float4* v;            // node velocity (global)
   const float2* mass;   // (1 / m, m)
   const float4* fcon;   // (dX, 1 / l0)
-  const float4* fclo;   // their FP32 remainders
   const int2* conn;
   const int32_t* rowptr;
   const int32_t* inc;
@@ -180,108 +181,41 @@ struct Rve {
   int64_t node_off, nt;
 };
 
-// Nodal internal force: incident fiber vectors, signed by the node's end.
-// The first kGatherWidth incidences are loaded with independent, predicated
-// loads so that a thread has all of them in flight at once (rows of a kNN
-// network hold ~2k entries); longer rows finish in a loop.
-constexpr int kGatherWidth = 8;
-
+// Nodal internal force: incident fiber vectors in the node's CSR order,
+// subtracted at a fiber's first end and added at its second.
 __device__ __forceinline__ void gather(const Rve& r, int i, float& a0, float& a1, float& a2) {
   a0 = 0.f; a1 = 0.f; a2 = 0.f;
   const int pb = __ldg(r.rowptr + i), pe = __ldg(r.rowptr + i + 1);
-  const int n = pe - pb;
-  int code[kGatherWidth];
-#pragma unroll
-  for (int j = 0; j < kGatherWidth; ++j) code[j] = (j < n) ? __ldg(r.inc + pb + j) : 0;
-  float4 t[kGatherWidth];
-#pragma unroll
-  for (int j = 0; j < kGatherWidth; ++j)
-    if (j < n) t[j] = r.n[code[j] >> 1];
-  // compensated (TwoSum) accumulation: the net force of a node is often a
-  // small difference of much larger fiber forces
-  float c0 = 0.f, c1 = 0.f, c2 = 0.f;
-#pragma unroll
-  for (int j = 0; j < kGatherWidth; ++j) {
-    if (j < n) {
-      const float s = (code[j] & 1) ? 1.f : -1.f;
-      float q, e;
-      two_sum(a0, s * t[j].x, q, e); a0 = q; c0 += e;
-      two_sum(a1, s * t[j].y, q, e); a1 = q; c1 += e;
-      two_sum(a2, s * t[j].z, q, e); a2 = q; c2 += e;
-    }
+  for (int p = pb; p < pe; ++p) {
+    const int code = __ldg(r.inc + p);
+    const float4 t = r.n[code >> 1];
+    const float sg = (code & 1) ? 1.f : -1.f;
+    a0 = fmaf(sg, t.x, a0);
+    a1 = fmaf(sg, t.y, a1);
+    a2 = fmaf(sg, t.z, a2);
   }
-  for (int p = pb + kGatherWidth; p < pe; ++p) {
-    const int cd = __ldg(r.inc + p);
-    const float4 tv = r.n[cd >> 1];
-    const float s = (cd & 1) ? 1.f : -1.f;
-    float q, e;
-    two_sum(a0, s * tv.x, q, e); a0 = q; c0 += e;
-    two_sum(a1, s * tv.y, q, e); a1 = q; c1 += e;
-    two_sum(a2, s * tv.z, q, e); a2 = q; c2 += e;
-  }
-  a0 += c0;
-  a1 += c1;
-  a2 += c2;
 }
 
-__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
-  p = a * b;
-  e = fmaf(a, b, -p);
-}
-
-// Green-strain numerator dX.du + du.du/2 of one fiber, accurate to a few
-// FP32 ulps of ITS OWN value. A fiber that mostly rotates has
-// dX.du ~ -du.du/2, and plain FP32 leaves an error ~ulp(|dX||du|): in
-// sub-isostatic networks such rotation-dominated fibers carry the soft modes,
-// which amplify that error into the stress. Here du is kept as an unevaluated
-// sum dh + dl (TwoSum of the hi parts plus the lo parts), the leading products
-// are split exactly with FMA (TwoProd) and the terms are added with
-// compensated (TwoSum) summation.
-__device__ __forceinline__ float strain_numerator(const float* X, const float* Xl,
-                                                  const float* dh, const float* dl) {
-  float S = 0.f, C = 0.f;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    float p, ep, q, eq, s, es;
-    two_prod(X[k], dh[k], p, ep);
-    const float hk = 0.5f * dh[k];
-    two_prod(hk, dh[k], q, eq);
-    two_sum(S, p, s, es);
-    S = s;
-    C += es + ep;
-    two_sum(S, q, s, es);
-    S = s;
-    C += es + eq;
-    C = fmaf(X[k] + dh[k], dl[k], C);  // dX dl + dh dl (dl^2 is below FP32 resolution)
-    C = fmaf(Xl[k], dh[k], C);         // remainder of dX times du
-  }
-  return S + C;
-}
-
+// Force vector of one fiber. The displacement difference du is formed with a
+// TwoSum of the hi parts plus the lo parts, so it is accurate to FP32 of du
+// itself; the Green strain follows from du (g l0^2 = du.(dX + du/2)), which
+// keeps its relative precision at small strain where 0.5(l^2/l0^2 - 1)
+// would cancel.
 __device__ __forceinline__ void fiber_force(const Rve& r, int e) {
   const int2 c = __ldg(r.conn + e);
-  float dh[3], dl[3];
+  float du[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     float d, ed;
     two_sum(r.hi(k, c.y), -r.hi(k, c.x), d, ed);
-    dh[k] = d;
-    dl[k] = ed + (r.lo(k, c.y) - r.lo(k, c.x));
+    du[k] = d + (ed + (r.lo(k, c.y) - r.lo(k, c.x)));
   }
   const float4 fc = __ldg(r.fcon + e);
-  const float4 fl = __ldg(r.fclo + e);
-  const float X[3] = {fc.x, fc.y, fc.z};
-  const float Xl[3] = {fl.x, fl.y, fl.z};
-  // 1/l0^2 and 1/l0 from the (hi, lo) pair
-  float r2, e2;
-  two_prod(fc.w, fc.w, r2, e2);
-  r2 = r2 + fmaf(2.f * fc.w, fl.w, e2);
-  const float rl0 = fc.w + fl.w;
-  const float g = strain_numerator(X, Xl, dh, dl) * r2;
-  const float t = tension_over_length(r.L, g, rl0);
-  r.n[e] = make_float4((X[0] + (dh[0] + (dl[0] + Xl[0]))) * t,
-                       (X[1] + (dh[1] + (dl[1] + Xl[1]))) * t,
-                       (X[2] + (dh[2] + (dl[2] + Xl[2]))) * t, 0.f);
+  const float gn = fmaf(du[0], fmaf(0.5f, du[0], fc.x),
+                        fmaf(du[1], fmaf(0.5f, du[1], fc.y), du[2] * fmaf(0.5f, du[2], fc.z)));
+  const float g = gn * (fc.w * fc.w);
+  const float t = tension_over_length(r.L, g, fc.w);
+  r.n[e] = make_float4((fc.x + du[0]) * t, (fc.y + du[1]) * t, (fc.z + du[2]) * t, 0.f);
 }
 
 // FP64 length of one fiber in the current configuration.
@@ -314,22 +248,21 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   const int64_t node_floats = 6LL * N, all_floats = 6LL * N + 4LL * E;
   if (all_floats <= smem_floats) {
     r.n = reinterpret_cast<float4*>(smem);
-    r.hi = {smem + 4 * E, N};
-    r.lo = {smem + 4 * E + 3 * N, N};
+    r.hi.set(smem + 4 * E, N);
+    r.lo.set(smem + 4 * E + 3 * N, N);
   } else if (node_floats <= smem_floats) {
     r.n = ms.nrm + fo;
-    r.hi = {smem, N};
-    r.lo = {smem + 3 * N, N};
+    r.hi.set(smem, N);
+    r.lo.set(smem + 3 * N, N);
   } else {
     r.n = ms.nrm + fo;
-    r.hi = {ms.u_hi + no, nt};
-    r.lo = {ms.u_lo + no, nt};
+    r.hi.set(ms.u_hi + no, nt);
+    r.lo.set(ms.u_lo + no, nt);
   }
   (void)et;
   r.v = ms.v + no;
   r.mass = ms.mass + no;
   r.fcon = ms.fcon + fo;
-  r.fclo = ms.fclo + fo;
   r.conn = b.conn + fo;
   r.rowptr = b.rowptr + d.row_off;
   r.inc = b.inc + d.inc_off;
@@ -571,8 +504,7 @@ void mixed_destroy(MixedState* ms) {
   if (!ms) return;
   for (void* p : {static_cast<void*>(ms->u_hi), static_cast<void*>(ms->u_lo),
                   static_cast<void*>(ms->v), static_cast<void*>(ms->mass),
-                  static_cast<void*>(ms->fcon), static_cast<void*>(ms->fclo),
-                  static_cast<void*>(ms->nrm)})
+                  static_cast<void*>(ms->fcon), static_cast<void*>(ms->nrm)})
     if (p) cudaFree(p);
   delete ms;
 }
@@ -586,7 +518,6 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
   if ((e = alloc(&ms.v, nt)) != cudaSuccess) return e;
   if ((e = alloc(&ms.mass, nt)) != cudaSuccess) return e;
   if ((e = alloc(&ms.fcon, et)) != cudaSuccess) return e;
-  if ((e = alloc(&ms.fclo, et)) != cudaSuccess) return e;
   if ((e = alloc(&ms.nrm, et)) != cudaSuccess) return e;
   ms.sms = sms;
   ms.smem_bytes = kSmemBytesMixed;
