@@ -55,7 +55,7 @@ struct MixedState {
 
 namespace {
 
-constexpr int kThreadsMixed = 512;
+constexpr int kThreadsMixed = 1024;
 constexpr int kSmemBytesMixed = 220 * 1024;
 
 __global__ void mixed_prepare_kernel(const DevBatch b, MixedState ms) {
