@@ -89,3 +89,31 @@ def test_mixed_incremental_and_transactional_runs(M):
         assert _rel(b.displacements(r), a.displacements(r)) <= REL_MIXED
     np.testing.assert_allclose(b.compute3DOrientationTensor(), a.compute3DOrientationTensor(),
                                rtol=0, atol=1e-9)
+
+
+def test_mixed_every_placement_and_cluster_size(M):
+    """One RVE per way the mixed solve places an RVE: all state in one CTA's
+    shared memory (800 nodes), node state only (6,000), node state split over
+    clusters of 2, 4 and 8 CTAs (14,000 / 30,000 / 50,000 nodes) and global
+    memory (80,000). Each agrees with FP64, and each gives the same bits
+    solved alone as in the mixed-size batch."""
+    from mumfim_gb300 import synthetic as S
+    sizes = (800, 6_000, 14_000, 30_000, 50_000, 80_000)
+    nets, F = [], []
+    for i, n in enumerate(sizes):
+        coords, conn = S.knn_network(n, 4, S.geometry_seed(7, i))
+        nets.append(M.FiberNetwork(coords, conn, [S._linear_params(7, i)]))
+        u = S.uniform(S.param_seed(7, i), 9) * 0.1 - 0.05
+        F.append(np.eye(3) + u.reshape(3, 3))
+    strat = [M.SolutionStrategy.ramp(1_000, 0.5) for _ in nets]
+    F = np.stack(F)
+    w = S.Workload("placements", nets, strat, F, 1_000)
+    g64, s64 = _solve(M, w, "f64")
+    g32, s32 = _solve(M, w, "mixed")
+    assert (g32.last_status["steps"] == 1_000).all()
+    for r in range(len(sizes)):
+        assert _rel(s32[r], s64[r]) <= REL_MIXED, r
+    for r in (0, 2, 4, 5):
+        one = w.subset([r])
+        _, s1 = _solve(M, one, "mixed")
+        np.testing.assert_array_equal(s1[0], s32[r])
