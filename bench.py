@@ -122,9 +122,15 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
-def build_workload(config: int, rank: int, n_rve: int | None, solve_steps: int | None = None):
+def build_workload(config: int, rank: int, n_rve: int | None, solve_steps: int | None = None,
+                   nodes: str | None = None):
     from mumfim_gb300 import synthetic as S
     kw = {"steps": solve_steps} if solve_steps else {}
+    if nodes:
+        if config != 2:
+            raise SystemExit("--nodes applies to config 2")
+        lo, hi = (int(v) for v in nodes.split(":"))
+        kw.update(n_min=lo, n_max=hi)
     if config == 1:
         n = n_rve or 1024
         w = S.config1(n_rve=n, first=rank * n, **kw)
@@ -132,7 +138,8 @@ def build_workload(config: int, rank: int, n_rve: int | None, solve_steps: int |
     elif config == 2:
         n = n_rve or 4096
         w = S.config2(n_rve=n, first=rank * n, **kw)
-        desc = (f"config2: {n} RVEs, nodes log-uniform [500,20000], k in {{3,4,5}}, linear law, "
+        band = f"[{kw.get('n_min', 500)},{kw.get('n_max', 20000)}]"
+        desc = (f"config2: {n} RVEs, nodes log-uniform {band}, k in {{3,4,5}}, linear law, "
                 f"F = I + U(+-0.08), {w.steps} ramp steps")
     elif config == 3:
         n = n_rve or 2048
@@ -176,7 +183,7 @@ def run_reference(args, rank, world):
     """CPU restatement of the reference path on the host cores (rank 0 only)."""
     if rank != 0:
         return
-    w, desc = build_workload(args.config, 0, args.n_rve, args.solve_steps)
+    w, desc = build_workload(args.config, 0, args.n_rve, args.solve_steps, args.nodes)
     threads = os.cpu_count() or 1
     from oracle import pyoracle
     sub = w.subset(range(min(args.cpu_sample_rves, w.n_rve)))
@@ -311,6 +318,8 @@ def main():
     ap.add_argument("--cpu-sample-rves", type=int, default=64)
     ap.add_argument("--solve-steps", type=int, default=None,
                     help="override the explicit steps per solve (small profiling cases)")
+    ap.add_argument("--nodes", default=None, metavar="LO:HI",
+                    help="config 2 with node counts log-uniform in [LO, HI] (profiling cases)")
     ap.add_argument("--f64-every", type=int, default=4)
     ap.add_argument("--serve-points", type=int, default=2048)
     ap.add_argument("--serve-steps", type=int, default=500)
@@ -341,7 +350,7 @@ def main():
     torch.cuda.set_device(local_rank)
     import mumfim_gb300 as m
 
-    w, desc = build_workload(args.config, rank, args.n_rve, args.solve_steps)
+    w, desc = build_workload(args.config, rank, args.n_rve, args.solve_steps, args.nodes)
     t0 = time.perf_counter()
     gpu = m.BatchedFiberRVEAnalysisExplicit(w.networks, w.strategies, precision=args.precision,
                                             device=local_rank)

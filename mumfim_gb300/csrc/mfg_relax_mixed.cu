@@ -50,29 +50,35 @@ namespace mfg {
 struct MixedState {
   float* u_hi = nullptr;   // 3 * nt (STREAM placement)
   float* u_lo = nullptr;   // 3 * nt
-  float4* v = nullptr;     // nt, velocity (w unused)
+  float* v = nullptr;      // 3 * nt, velocity (STREAM placement)
   float2* mass = nullptr;  // nt, (1 / m, m)
   float4* fcon = nullptr;  // et, (X[n2] - X[n1], 1 / l0) rounded to FP32
   float4* nrm = nullptr;   // et, per-fiber force vectors (scratch; w unused)
   int sms = 1;
   int smem_bytes = 0;
-  // Size buckets of the batch run: bucket q is solved by clusters of
-  // kClusterSizes[q] CTAs; its RVEs, most fibers first, are
+  // Size buckets of the batch run (kBucket[q]: cluster size, force vectors
+  // in shared memory); the RVEs of bucket q, most fibers first, are
   // order[bucket_off[q] .. bucket_off[q + 1]).
   int32_t* order = nullptr;
   int32_t* queues = nullptr;  // one claim counter per bucket
-  int bucket_off[5] = {0, 0, 0, 0, 0};
-  int bucket_grid[4] = {0, 0, 0, 0};
-  cudaStream_t side[4] = {nullptr, nullptr, nullptr, nullptr};
+  int bucket_off[6] = {0, 0, 0, 0, 0, 0};
+  int bucket_grid[5] = {0, 0, 0, 0, 0};
+  cudaStream_t side[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t fork = nullptr;
-  cudaEvent_t join[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t join[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 };
 
 namespace {
 
 constexpr int kThreadsMixed = 1024;
 constexpr int kSmemBytesMixed = 220 * 1024;
-constexpr int kClusterSizes[4] = {8, 4, 2, 1};
+// Size buckets, launched in this order (largest clusters first).
+struct BucketKind {
+  int cl;    // CTAs per cluster
+  bool all;  // fiber force vectors in shared memory too
+};
+constexpr int kBuckets = 5;
+constexpr BucketKind kBucket[kBuckets] = {{8, false}, {4, false}, {4, true}, {2, true}, {1, true}};
 
 __global__ void mixed_prepare_kernel(const DevBatch b, MixedState ms) {
   const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
@@ -185,8 +191,8 @@ struct Field3 {
 struct Rve {
   RveDesc d;
   Law L;
-  float4* n;            // fiber force vectors
-  float4* v;            // node velocity (global)
+  float4* n;            // this CTA's fiber force vectors, indexed by slot - e_base
+  int e_base;
   const float2* mass;   // (1 / m, m)
   const float4* fcon;   // (dX, 1 / l0)
   const int2* conn;
@@ -195,6 +201,22 @@ struct Rve {
   float* ramp;          // per boundary node: step increment d/n as (hi[3], lo[3])
   int64_t node_off, nt;
 };
+
+// Owner of element j of a field split into CL blocks of `chunk`.
+template <int CL>
+__device__ __forceinline__ int owner(int j, int chunk) {
+  int o = 0;
+#pragma unroll
+  for (int q = 1; q < CL; ++q) o += (j >= q * chunk) ? 1 : 0;
+  return o;
+}
+
+// Shared-window address of `local` in CTA `o` of this cluster.
+__device__ __forceinline__ uint32_t cluster_addr(uint32_t local, int o) {
+  uint32_t remote;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(local), "r"(o));
+  return remote;
+}
 
 // Node displacement (hi, lo) of an RVE solved by one CTA: in its shared
 // memory (resident placements) or in global memory (streaming placement).
@@ -213,21 +235,29 @@ struct LocalNodes {
 };
 
 // Node displacement of an RVE split over the CL CTAs of a thread-block
-// cluster, read through distributed shared memory: CTA o holds nodes
-// [o*chunk, (o+1)*chunk) as six blocks of `chunk` floats (hi x, y, z, lo x,
-// y, z) at the same shared-memory offset `base` in every CTA.
+// cluster, read through distributed shared memory. The free nodes [0, nf)
+// and the boundary nodes [nf, N) are split separately into CL contiguous
+// blocks of fchunk and bchunk (both segments are Morton-sorted, so CTA o gets
+// the free and the boundary nodes of the same region of the RVE). CTA o keeps
+// its free nodes at local index 0.. and its boundary nodes at fchunk.., in six
+// component arrays of `cap` floats (hi x, y, z, lo x, y, z) at the same
+// shared-memory offset `base` in every CTA.
 template <int CL>
 struct ClusterNodes {
   uint32_t base;  // shared-window address of this CTA's block
-  int chunk;
+  int fchunk, bchunk, nf, cap;
   __device__ __forceinline__ void load(int j, float (&uh)[3], float (&ul)[3]) const {
-    int o = 0;
-#pragma unroll
-    for (int q = 1; q < CL; ++q) o += (j >= q * chunk) ? 1 : 0;
-    const uint32_t local = base + 4u * static_cast<uint32_t>(j - o * chunk);
-    uint32_t remote;
-    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(local), "r"(o));
-    const uint32_t stride = 4u * static_cast<uint32_t>(chunk);
+    int o, local;
+    if (j < nf) {
+      o = owner<CL>(j, fchunk);
+      local = j - o * fchunk;
+    } else {
+      const int jb = j - nf;
+      o = owner<CL>(jb, bchunk);
+      local = fchunk + jb - o * bchunk;
+    }
+    const uint32_t remote = cluster_addr(base + 4u * static_cast<uint32_t>(local), o);
+    const uint32_t stride = 4u * static_cast<uint32_t>(cap);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(uh[k]) : "r"(remote + k * stride));
@@ -238,6 +268,29 @@ struct ClusterNodes {
   }
 };
 
+// Fiber force vectors in one CTA's shared memory or in global memory.
+struct LocalForces {
+  const float4* p;
+  __device__ __forceinline__ float4 load(int e) const { return p[e]; }
+};
+
+// Fiber force vectors of an RVE split over a cluster: CTA o holds slots
+// [o*echunk, (o+1)*echunk) as float4 at shared-memory offset 0.
+template <int CL>
+struct ClusterForces {
+  uint32_t base;
+  int echunk;
+  __device__ __forceinline__ float4 load(int e) const {
+    const int o = owner<CL>(e, echunk);
+    const uint32_t a = cluster_addr(base + 16u * static_cast<uint32_t>(e - o * echunk), o);
+    float4 t;
+    asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(t.x), "=f"(t.y), "=f"(t.z), "=f"(t.w)
+                 : "r"(a));
+    return t;
+  }
+};
+
 template <int CL>
 struct ClusterOps {
   __device__ static int rank() {
@@ -245,7 +298,7 @@ struct ClusterOps {
     return 0;
   }
   // Block barrier, or cluster barrier (release / acquire at cluster scope,
-  // which also orders the global-memory force vectors between CTAs).
+  // which also orders global-memory force vectors between CTAs).
   __device__ static void sync() {
     if constexpr (CL > 1)
       cg::this_cluster().sync();
@@ -276,12 +329,31 @@ struct ClusterOps {
 
 // Nodal internal force: incident fiber vectors in the node's CSR order,
 // subtracted at a fiber's first end and added at its second.
-__device__ __forceinline__ void gather(const Rve& r, int i, float& a0, float& a1, float& a2) {
+template <class Forces>
+__device__ __forceinline__ void gather(const Rve& r, const Forces& fv, int i, float& a0, float& a1,
+                                       float& a2) {
   a0 = 0.f; a1 = 0.f; a2 = 0.f;
   const int pb = __ldg(r.rowptr + i), pe = __ldg(r.rowptr + i + 1);
-  for (int p = pb; p < pe; ++p) {
+  int p = pb;
+  // four incidences in flight, summed in CSR order
+  for (; p + 4 <= pe; p += 4) {
+    int code[4];
+    float4 t[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) code[q] = __ldg(r.inc + p + q);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) t[q] = fv.load(code[q] >> 1);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float sg = (code[q] & 1) ? 1.f : -1.f;
+      a0 = fmaf(sg, t[q].x, a0);
+      a1 = fmaf(sg, t[q].y, a1);
+      a2 = fmaf(sg, t[q].z, a2);
+    }
+  }
+  for (; p < pe; ++p) {
     const int code = __ldg(r.inc + p);
-    const float4 t = r.n[code >> 1];
+    const float4 t = fv.load(code >> 1);
     const float sg = (code & 1) ? 1.f : -1.f;
     a0 = fmaf(sg, t.x, a0);
     a1 = fmaf(sg, t.y, a1);
@@ -312,7 +384,8 @@ __device__ __forceinline__ void fiber_force(const Rve& r, const Nodes& u, int e)
                         fmaf(du[1], fmaf(0.5f, du[1], fc.y), du[2] * fmaf(0.5f, du[2], fc.z)));
   const float g = gn * (fc.w * fc.w);
   const float t = tension_over_length(r.L, g, fc.w);
-  r.n[e] = make_float4((fc.x + du[0]) * t, (fc.y + du[1]) * t, (fc.z + du[2]) * t, 0.f);
+  r.n[e - r.e_base] =
+      make_float4((fc.x + du[0]) * t, (fc.y + du[1]) * t, (fc.z + du[2]) * t, 0.f);
 }
 
 // FP64 length of one fiber in the current configuration.
@@ -333,10 +406,27 @@ __device__ __forceinline__ double length64(const Rve& r, const Nodes& u, const d
   return sqrt(s2);
 }
 
-// One RVE solved by one CTA (CL = 1) or by the CL CTAs of a cluster, each
-// owning a contiguous range of nodes (storage order is Morton-sorted, so a
-// range is a compact region of the RVE) and a range of fiber slots.
-template <int CL>
+// Shared-memory floats of an RVE solved by a cluster of CL CTAs: 9 per node
+// slot of a CTA (displacement hi, lo and velocity; ceil(NF/CL) free plus
+// ceil(NB/CL) boundary slots), plus 4 per fiber slot (ceil(E/CL)) when the
+// force vectors are kept in shared memory too (all).
+__host__ __device__ inline int64_t cluster_floats(int n_nodes, int n_free, int n_fibers, int cl,
+                                                  bool all) {
+  const int64_t nb = n_nodes - n_free;
+  const int64_t cap = (static_cast<int64_t>(n_free) + cl - 1) / cl + (nb + cl - 1) / cl;
+  const int64_t echunk = (static_cast<int64_t>(n_fibers) + cl - 1) / cl;
+  return 9 * cap + (all ? 4 * echunk : 0);
+}
+
+// One RVE solved by one CTA (CL = 1) or by the CL CTAs of a cluster. A CTA
+// of a cluster owns a contiguous range of nodes (storage order is Morton-
+// sorted, so a range is a compact region of the RVE) with their displacement
+// and velocity in its shared memory, and a range of fiber slots whose force
+// vectors it computes: in its shared memory when kAll, else in global memory.
+// A single CTA places the RVE by its size: everything in shared memory,
+// the node state only, the displacements only, or everything in global
+// memory.
+template <int CL, bool kAll>
 __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const RunArgs& a, int rve,
                                 double* red, double* cred, float* smem, int smem_floats) {
   using Ops = ClusterOps<CL>;
@@ -350,39 +440,69 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   r.node_off = no;
   r.nt = nt;
   const int rank = Ops::rank();
-  const int chunk = (N + CL - 1) / CL;
-  const int n_lo = CL > 1 ? min(N, rank * chunk) : 0;
-  const int n_hi = CL > 1 ? min(N, n_lo + chunk) : N;
-  const int e_lo = static_cast<int>(static_cast<int64_t>(E) * rank / CL);
-  const int e_hi = static_cast<int>(static_cast<int64_t>(E) * (rank + 1) / CL);
+  const int NB = N - NF;
+  const int fchunk = (NF + CL - 1) / CL, bchunk = (NB + CL - 1) / CL, cap = fchunk + bchunk;
+  // own free nodes [f_lo, f_hi) at local index i - f_lo, own boundary nodes
+  // [g_lo, g_hi) at local index fchunk + i - g_lo (with CL = 1 both are i)
+  const int f_lo = min(NF, rank * fchunk), f_hi = min(NF, f_lo + fchunk);
+  const int g_lo = NF + min(NB, rank * bchunk), g_hi = NF + min(NB, rank * bchunk + bchunk);
+  const int nfo = f_hi - f_lo, n_own = nfo + (g_hi - g_lo);
+  const int echunk = (E + CL - 1) / CL;
+  const int e_lo = min(E, rank * echunk);
+  const int e_hi = min(E, e_lo + echunk);
   using Nodes = std::conditional_t<(CL > 1), ClusterNodes<CL>, LocalNodes>;
-  Nodes u;        // every node of the RVE (fiber pass)
-  LocalNodes own;  // the nodes this CTA updates, by index - n_lo
+  using Forces = std::conditional_t<(CL > 1 && kAll), ClusterForces<CL>, LocalForces>;
+  Nodes u;         // every node of the RVE (fiber pass)
+  LocalNodes own;  // the nodes this CTA updates, by local index
+  Field3 vel;      // their velocities, by local index
+  Forces fv;       // every fiber force vector of the RVE (node pass)
+  r.e_base = 0;
   if constexpr (CL > 1) {
-    r.n = ms.nrm + fo;
-    u.chunk = chunk;
-    u.base = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
-    own.h.set(smem, chunk);
-    own.l.set(smem + 3 * chunk, chunk);
+    float* nodes = smem;
+    if constexpr (kAll) {
+      r.n = reinterpret_cast<float4*>(smem);
+      r.e_base = e_lo;
+      fv.base = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+      fv.echunk = echunk;
+      nodes = smem + 4 * echunk;
+    } else {
+      r.n = ms.nrm + fo;
+      fv.p = r.n;
+    }
+    u.base = static_cast<uint32_t>(__cvta_generic_to_shared(nodes));
+    u.fchunk = fchunk;
+    u.bchunk = bchunk;
+    u.nf = NF;
+    u.cap = cap;
+    own.h.set(nodes, cap);
+    own.l.set(nodes + 3 * cap, cap);
+    vel.set(nodes + 6 * cap, cap);
   } else {
-    // placement: force vectors first (16-byte aligned), then the node fields
-    const int64_t node_floats = 6LL * N, all_floats = 6LL * N + 4LL * E;
-    if (all_floats <= smem_floats) {
+    // force vectors first (16-byte aligned), then the node fields
+    if (cluster_floats(N, NF, E, 1, true) <= smem_floats) {
       r.n = reinterpret_cast<float4*>(smem);
       own.h.set(smem + 4 * E, N);
       own.l.set(smem + 4 * E + 3 * N, N);
-    } else if (node_floats <= smem_floats) {
+      vel.set(smem + 4 * E + 6 * N, N);
+    } else if (cluster_floats(N, NF, E, 1, false) <= smem_floats) {
       r.n = ms.nrm + fo;
       own.h.set(smem, N);
       own.l.set(smem + 3 * N, N);
+      vel.set(smem + 6 * N, N);
+    } else if (6LL * N <= smem_floats) {
+      r.n = ms.nrm + fo;
+      own.h.set(smem, N);
+      own.l.set(smem + 3 * N, N);
+      vel.set(ms.v + no, nt);
     } else {
       r.n = ms.nrm + fo;
       own.h.set(ms.u_hi + no, nt);
       own.l.set(ms.u_lo + no, nt);
+      vel.set(ms.v + no, nt);
     }
+    fv.p = r.n;
     u = own;
   }
-  r.v = ms.v + no;
   r.mass = ms.mass + no;
   r.fcon = ms.fcon + fo;
   r.conn = b.conn + fo;
@@ -397,7 +517,9 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   if (a.update_coords && rank == 0 && tid == 0) b.vol[rve] = jacobian(Fm) * b.vol[rve];
 
   // ---- prologue in FP64: predictor, split into (hi, lo), v = 0 -------------
-  for (int i = n_lo + tid; i < n_hi; i += kThreadsMixed) {
+  for (int t = tid; t < n_own; t += kThreadsMixed) {
+    const int i = t < nfo ? f_lo + t : g_lo + (t - nfo);
+    const int li = t < nfo ? t : fchunk + (t - nfo);
     double xo[3], up[3], X[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -417,10 +539,10 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
       xn[k] = X[k] + up[k];
       float hi, lo;
       split(xn[k] - X[k], hi, lo);
-      own.hi(k, i - n_lo) = hi;
-      own.lo(k, i - n_lo) = lo;
+      own.hi(k, li) = hi;
+      own.lo(k, li) = lo;
+      vel(k, li) = 0.f;
     }
-    r.v[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (ramp && i >= NF) {
       // The boundary moves by d/n per step, d = (F - I) x0. The increment is
       // kept as an exact FP32 pair and accumulated without rounding into
@@ -448,11 +570,9 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   double dt_crit =
       Ops::template combine<true>(block_min<kThreadsMixed>(lmin, red), cred) / d.sound_speed;
 
-  const int cap = d.max_steps;
+  const int step_cap = d.max_steps;
   const float c = static_cast<float>(d.c);
   float h_cur = static_cast<float>(d.crit * dt_crit * 0.5);
-  const int f_hi = min(n_hi, NF);  // own free nodes [n_lo, f_hi)
-  const int b_lo = max(n_lo, NF);  // own boundary nodes [b_lo, n_hi)
   int step = 0;
   double residual = 10.0;
   float h_prev = 0.f;
@@ -461,9 +581,9 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
     const bool res_step = step > 0 && ((step - 1) % kUpdateFreq) == 0;
     if (res_step) {
       double part = 0.0;
-      for (int i = n_lo + tid; i < f_hi; i += kThreadsMixed) {
+      for (int i = f_lo + tid; i < f_hi; i += kThreadsMixed) {
         float a0, a1, a2;
-        gather(r, i, a0, a1, a2);
+        gather(r, fv, i, a0, a1, a2);
         part += static_cast<double>(a0) * a0 + static_cast<double>(a1) * a1 +
                 static_cast<double>(a2) * a2;
       }
@@ -474,40 +594,39 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
       }
     }
     if (!ramp && res_step && !(residual > d.tol)) break;
-    if (step >= cap) break;
+    if (step >= step_cap) break;
     // per-step scalars in FP32 (h changes only when dt_crit does)
     const float h = h_cur;
     const float hk = h_prev + h;  // trailing kick of step-1 + leading kick of step
     const float h2 = h + h;
-    for (int i = n_lo + tid; i < f_hi; i += kThreadsMixed) {
+    for (int i = f_lo + tid; i < f_hi; i += kThreadsMixed) {
       float f[3];
-      gather(r, i, f[0], f[1], f[2]);
+      gather(r, fv, i, f[0], f[1], f[2]);
       const float2 mm = __ldg(r.mass + i);
       const float mc = mm.y * c;
       const float km = hk * mm.x;
-      float4 w = r.v[i];
-      w.x = fmaf(km, -f[0] - mc * w.x, w.x);
-      w.y = fmaf(km, -f[1] - mc * w.y, w.y);
-      w.z = fmaf(km, -f[2] - mc * w.z, w.z);
-      r.v[i] = w;
-      const float wk[3] = {w.x, w.y, w.z};
+      const int li = i - f_lo;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        float hi = own.hi(k, i - n_lo), lo = own.lo(k, i - n_lo);
-        comp_add(hi, lo, h2 * wk[k]);
-        own.hi(k, i - n_lo) = hi;
-        own.lo(k, i - n_lo) = lo;
+        float w = vel(k, li);
+        w = fmaf(km, -f[k] - mc * w, w);
+        vel(k, li) = w;
+        float hi = own.hi(k, li), lo = own.lo(k, li);
+        comp_add(hi, lo, h2 * w);
+        own.hi(k, li) = hi;
+        own.lo(k, li) = lo;
       }
     }
     if (ramp) {
-      for (int i = b_lo + tid; i < n_hi; i += kThreadsMixed) {
+      for (int i = g_lo + tid; i < g_hi; i += kThreadsMixed) {
         const float* rb = r.ramp + 12 * (i - NF);
+        const int li = fchunk + (i - g_lo);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
           float s, e;
-          two_sum(own.hi(k, i - n_lo), rb[k], s, e);
-          own.hi(k, i - n_lo) = s;
-          own.lo(k, i - n_lo) = own.lo(k, i - n_lo) + (e + rb[3 + k]);
+          two_sum(own.hi(k, li), rb[k], s, e);
+          own.hi(k, li) = s;
+          own.lo(k, li) = own.lo(k, li) + (e + rb[3 + k]);
         }
       }
     }
@@ -537,17 +656,19 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   if (status == 0 && !ramp && residual > d.tol) status = 3;
 
   // ---- finalize: FP64 positions, boundary f_int, stress ---------------------
-  for (int i = n_lo + tid; i < n_hi; i += kThreadsMixed) {
+  for (int t = tid; t < n_own; t += kThreadsMixed) {
+    const int i = t < nfo ? f_lo + t : g_lo + (t - nfo);
+    const int li = t < nfo ? t : fchunk + (t - nfo);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       const double Xk = b.X[k * nt + no + i];
-      const double xk = Xk + (static_cast<double>(own.hi(k, i - n_lo)) + own.lo(k, i - n_lo));
+      const double xk = Xk + (static_cast<double>(own.hi(k, li)) + own.lo(k, li));
       b.x[k * nt + no + i] = xk;
       if (a.update_coords) b.u[k * nt + no + i] = xk - Xk;
     }
     if (i >= NF) {
       float a0, a1, a2;
-      gather(r, i, a0, a1, a2);
+      gather(r, fv, i, a0, a1, a2);
       b.fint[no + i] = a0;
       b.fint[nt + no + i] = a1;
       b.fint[2 * nt + no + i] = a2;
@@ -592,11 +713,12 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
 
 // Persistent relaxation over one size bucket: CTA (or cluster) after cluster
 // takes the next RVE of `order` (largest first) until the bucket is empty.
-template <int CL>
+template <int CL, bool kAll>
 __global__ void __launch_bounds__(kThreadsMixed, 1)
 relax_mixed_kernel(const DevBatch b, const MixedState ms, const RunArgs a, int smem_floats,
                    const int32_t* order, int n_order, int32_t* queue) {
-  extern __shared__ float smem[];
+  extern __shared__ float4 smem4[];
+  float* smem = reinterpret_cast<float*>(smem4);
   __shared__ double red[kThreadsMixed / 32 + 1];
   __shared__ double cred[1];
   __shared__ int s_rve;
@@ -617,17 +739,18 @@ relax_mixed_kernel(const DevBatch b, const MixedState ms, const RunArgs a, int s
       __syncthreads();
     }
     if (rve < 0) break;
-    solve_rve_mixed<CL>(b, ms, a, rve, red, cred, smem, smem_floats);
+    solve_rve_mixed<CL, kAll>(b, ms, a, rve, red, cred, smem, smem_floats);
   }
 }
 
 __global__ void __launch_bounds__(kThreadsMixed, 1)
 server_mixed_kernel(const DevBatch b, const MixedState ms, const ServerArgs sa, int smem_floats) {
-  extern __shared__ float smem[];
+  extern __shared__ float4 smem4[];
+  float* smem = reinterpret_cast<float*>(smem4);
   __shared__ double red[kThreadsMixed / 32 + 1];
   __shared__ double cred[1];
   server_loop(sa, [&](const RunArgs& a, int rve) {
-    solve_rve_mixed<1>(b, ms, a, rve, red, cred, smem, smem_floats);
+    solve_rve_mixed<1, true>(b, ms, a, rve, red, cred, smem, smem_floats);
   });
 }
 
@@ -647,7 +770,7 @@ void mixed_destroy(MixedState* ms) {
                   static_cast<void*>(ms->fcon), static_cast<void*>(ms->nrm),
                   static_cast<void*>(ms->order), static_cast<void*>(ms->queues)})
     if (p) cudaFree(p);
-  for (int q = 0; q < 4; ++q) {
+  for (int q = 0; q < kBuckets; ++q) {
     if (ms->side[q]) cudaStreamDestroy(ms->side[q]);
     if (ms->join[q]) cudaEventDestroy(ms->join[q]);
   }
@@ -657,54 +780,71 @@ void mixed_destroy(MixedState* ms) {
 
 namespace {
 
-// Bucket of an RVE: the smallest cluster whose CTAs hold its node
-// displacements (24 B per node) in shared memory; RVEs too large even for
-// the largest cluster are solved by one CTA from global memory.
+// Bucket of an RVE: one CTA if all its mutable state (displacement hi, lo,
+// velocity, fiber force vectors) fits in its shared memory, else the
+// smallest cluster of 2 or 4 over which it fits, else clusters of 4, then 8,
+// holding the node state only, else one CTA that keeps what fits in shared
+// memory and streams the rest from global memory. Clusters of 8 are the last
+// resort: with 220 KB per CTA only 15 of them (120 SMs) are resident at once,
+// against 36 clusters of 4 (144 SMs).
 int bucket_of(const RveDesc& d, int smem_floats) {
-  for (int q = 3; q >= 0; --q) {
-    const int cl = kClusterSizes[q];
-    const int64_t chunk = (static_cast<int64_t>(d.n_nodes) + cl - 1) / cl;
-    if (6 * chunk <= smem_floats) return q;
-  }
-  return 3;
+  static const int pref[] = {4, 3, 2, 1, 0};
+  for (int q : pref)
+    if (cluster_floats(d.n_nodes, d.n_free, d.n_fibers, kBucket[q].cl, kBucket[q].all) <=
+        smem_floats)
+      return q;
+  return kBuckets - 1;
 }
 
-template <int CL>
-cudaError_t launch_bucket(const MixedState& ms, const DevBatch& b, const RunArgs& a, int q,
-                          cudaStream_t s) {
-  const int n = ms.bucket_off[q + 1] - ms.bucket_off[q];
+template <int CL, bool kAll>
+cudaLaunchConfig_t launch_config(const MixedState& ms, unsigned grid, cudaStream_t s,
+                                 cudaLaunchAttribute* attr) {
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(static_cast<unsigned>(ms.bucket_grid[q]), 1, 1);
+  cfg.gridDim = dim3(grid, 1, 1);
   cfg.blockDim = dim3(kThreadsMixed, 1, 1);
   cfg.dynamicSmemBytes = static_cast<size_t>(ms.smem_bytes);
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = CL;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = CL > 1 ? 1 : 0;
-  return cudaLaunchKernelEx(&cfg, relax_mixed_kernel<CL>, b, ms, a,
+  return cfg;
+}
+
+template <int CL, bool kAll>
+cudaError_t launch_bucket(const MixedState& ms, const DevBatch& b, const RunArgs& a, int q,
+                          cudaStream_t s) {
+  const int n = ms.bucket_off[q + 1] - ms.bucket_off[q];
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg =
+      launch_config<CL, kAll>(ms, static_cast<unsigned>(ms.bucket_grid[q]), s, attr);
+  return cudaLaunchKernelEx(&cfg, relax_mixed_kernel<CL, kAll>, b, ms, a,
                             static_cast<int>(ms.smem_bytes / sizeof(float)),
                             static_cast<const int32_t*>(ms.order + ms.bucket_off[q]), n,
                             ms.queues + q);
 }
 
-template <int CL>
-cudaError_t max_clusters(const MixedState& ms, int* out) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(static_cast<unsigned>(CL * ms.sms), 1, 1);
-  cfg.blockDim = dim3(kThreadsMixed, 1, 1);
-  cfg.dynamicSmemBytes = static_cast<size_t>(ms.smem_bytes);
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = CL;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaOccupancyMaxActiveClusters(out, relax_mixed_kernel<CL>, &cfg);
+template <int CL, bool kAll>
+cudaError_t setup_bucket(MixedState& ms, int n, int q) {
+  cudaError_t e = cudaFuncSetAttribute(relax_mixed_kernel<CL, kAll>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       ms.smem_bytes);
+  if (e != cudaSuccess) return e;
+  int clusters = ms.sms;
+  if (CL > 1 && n > 0) {
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg =
+        launch_config<CL, kAll>(ms, static_cast<unsigned>(CL * ms.sms), nullptr, attr);
+    clusters = 0;
+    if ((e = cudaOccupancyMaxActiveClusters(&clusters, relax_mixed_kernel<CL, kAll>, &cfg)) !=
+        cudaSuccess)
+      return e;
+    if (clusters < 1) return cudaErrorInvalidConfiguration;
+  }
+  ms.bucket_grid[q] = CL * std::min(n, clusters);
+  return cudaSuccess;
 }
 
 }  // namespace
@@ -715,63 +855,46 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
   const size_t nt = static_cast<size_t>(b.nt), et = static_cast<size_t>(b.et);
   if ((e = alloc(&ms.u_hi, 3 * nt)) != cudaSuccess) return e;
   if ((e = alloc(&ms.u_lo, 3 * nt)) != cudaSuccess) return e;
-  if ((e = alloc(&ms.v, nt)) != cudaSuccess) return e;
+  if ((e = alloc(&ms.v, 3 * nt)) != cudaSuccess) return e;
   if ((e = alloc(&ms.mass, nt)) != cudaSuccess) return e;
   if ((e = alloc(&ms.fcon, et)) != cudaSuccess) return e;
   if ((e = alloc(&ms.nrm, et)) != cudaSuccess) return e;
   if ((e = alloc(&ms.order, desc.size())) != cudaSuccess) return e;
-  if ((e = alloc(&ms.queues, 4)) != cudaSuccess) return e;
+  if ((e = alloc(&ms.queues, kBuckets)) != cudaSuccess) return e;
   ms.sms = sms;
   ms.smem_bytes = kSmemBytesMixed;
   const int smem_floats = kSmemBytesMixed / static_cast<int>(sizeof(float));
-  if ((e = cudaFuncSetAttribute(relax_mixed_kernel<1>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytesMixed)) !=
-          cudaSuccess ||
-      (e = cudaFuncSetAttribute(relax_mixed_kernel<2>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytesMixed)) !=
-          cudaSuccess ||
-      (e = cudaFuncSetAttribute(relax_mixed_kernel<4>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytesMixed)) !=
-          cudaSuccess ||
-      (e = cudaFuncSetAttribute(relax_mixed_kernel<8>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytesMixed)) !=
-          cudaSuccess ||
-      (e = cudaFuncSetAttribute(server_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if ((e = cudaFuncSetAttribute(server_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 kSmemBytesMixed)) != cudaSuccess)
     return e;
 
   // size buckets, each in longest-processing-time order
-  std::vector<std::vector<int32_t>> bucket(4);
+  std::vector<std::vector<int32_t>> bucket(kBuckets);
   for (size_t r = 0; r < desc.size(); ++r)
     bucket[bucket_of(desc[r], smem_floats)].push_back(static_cast<int32_t>(r));
   std::vector<int32_t> order;
   order.reserve(desc.size());
-  for (int q = 0; q < 4; ++q) {
+  for (int q = 0; q < kBuckets; ++q) {
     std::stable_sort(bucket[q].begin(), bucket[q].end(),
                      [&](int32_t x, int32_t y) { return desc[x].n_fibers > desc[y].n_fibers; });
     ms.bucket_off[q] = static_cast<int>(order.size());
     order.insert(order.end(), bucket[q].begin(), bucket[q].end());
   }
-  ms.bucket_off[4] = static_cast<int>(order.size());
+  ms.bucket_off[kBuckets] = static_cast<int>(order.size());
   if (!order.empty() &&
       (e = cudaMemcpyAsync(ms.order, order.data(), order.size() * sizeof(int32_t),
                            cudaMemcpyHostToDevice, s)) != cudaSuccess)
     return e;
-  for (int q = 0; q < 4; ++q) {
+  for (int q = 0; q < kBuckets; ++q) {
     const int n = ms.bucket_off[q + 1] - ms.bucket_off[q];
-    const int cl = kClusterSizes[q];
-    int clusters = sms / cl;
-    if (n > 0 && cl > 1) {
-      clusters = 0;
-      switch (cl) {
-        case 8: e = max_clusters<8>(ms, &clusters); break;
-        case 4: e = max_clusters<4>(ms, &clusters); break;
-        default: e = max_clusters<2>(ms, &clusters); break;
-      }
-      if (e != cudaSuccess) return e;
-      if (clusters < 1) return cudaErrorInvalidConfiguration;
+    switch (q) {
+      case 0: e = setup_bucket<kBucket[0].cl, kBucket[0].all>(ms, n, q); break;
+      case 1: e = setup_bucket<kBucket[1].cl, kBucket[1].all>(ms, n, q); break;
+      case 2: e = setup_bucket<kBucket[2].cl, kBucket[2].all>(ms, n, q); break;
+      case 3: e = setup_bucket<kBucket[3].cl, kBucket[3].all>(ms, n, q); break;
+      default: e = setup_bucket<kBucket[4].cl, kBucket[4].all>(ms, n, q); break;
     }
-    ms.bucket_grid[q] = cl * std::min(n, std::max(clusters, 1));
+    if (e != cudaSuccess) return e;
     if ((e = cudaStreamCreateWithFlags(&ms.side[q], cudaStreamNonBlocking)) != cudaSuccess)
       return e;
     if ((e = cudaEventCreateWithFlags(&ms.join[q], cudaEventDisableTiming)) != cudaSuccess)
@@ -804,17 +927,19 @@ cudaError_t run_mixed(MixedState& ms, const DevBatch& b, const RunArgs& a, cudaS
                       int* launches) {
   cudaError_t e;
   *launches = 0;
-  if ((e = cudaMemsetAsync(ms.queues, 0, 4 * sizeof(int32_t), s)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(ms.queues, 0, kBuckets * sizeof(int32_t), s)) != cudaSuccess)
+    return e;
   if ((e = cudaEventRecord(ms.fork, s)) != cudaSuccess) return e;
-  for (int q = 0; q < 4; ++q) {
+  for (int q = 0; q < kBuckets; ++q) {
     if (ms.bucket_off[q + 1] == ms.bucket_off[q]) continue;
     cudaStream_t sq = ms.side[q];
     if ((e = cudaStreamWaitEvent(sq, ms.fork, 0)) != cudaSuccess) return e;
-    switch (kClusterSizes[q]) {
-      case 8: e = launch_bucket<8>(ms, b, a, q, sq); break;
-      case 4: e = launch_bucket<4>(ms, b, a, q, sq); break;
-      case 2: e = launch_bucket<2>(ms, b, a, q, sq); break;
-      default: e = launch_bucket<1>(ms, b, a, q, sq); break;
+    switch (q) {
+      case 0: e = launch_bucket<kBucket[0].cl, kBucket[0].all>(ms, b, a, q, sq); break;
+      case 1: e = launch_bucket<kBucket[1].cl, kBucket[1].all>(ms, b, a, q, sq); break;
+      case 2: e = launch_bucket<kBucket[2].cl, kBucket[2].all>(ms, b, a, q, sq); break;
+      case 3: e = launch_bucket<kBucket[3].cl, kBucket[3].all>(ms, b, a, q, sq); break;
+      default: e = launch_bucket<kBucket[4].cl, kBucket[4].all>(ms, b, a, q, sq); break;
     }
     if (e != cudaSuccess) return e;
     ++*launches;

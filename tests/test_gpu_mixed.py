@@ -92,13 +92,13 @@ def test_mixed_incremental_and_transactional_runs(M):
 
 
 def test_mixed_every_placement_and_cluster_size(M):
-    """One RVE per way the mixed solve places an RVE: all state in one CTA's
-    shared memory (800 nodes), node state only (6,000), node state split over
-    clusters of 2, 4 and 8 CTAs (14,000 / 30,000 / 50,000 nodes) and global
-    memory (80,000). Each agrees with FP64, and each gives the same bits
-    solved alone as in the mixed-size batch."""
+    """One RVE per way a batch run places an RVE: all mutable state in one
+    CTA's shared memory (800 nodes), all of it split over clusters of 2 and 4
+    CTAs (4,000 / 9,000 nodes), node state only over clusters of 4 and 8
+    (20,000 / 40,000) and global memory (80,000). Each agrees with FP64, and
+    each gives the same bits solved alone as in the mixed-size batch."""
     from mumfim_gb300 import synthetic as S
-    sizes = (800, 6_000, 14_000, 30_000, 50_000, 80_000)
+    sizes = (800, 4_000, 9_000, 20_000, 40_000, 80_000)
     nets, F = [], []
     for i, n in enumerate(sizes):
         coords, conn = S.knn_network(n, 4, S.geometry_seed(7, i))

@@ -102,3 +102,31 @@ def test_admission_ring_full_and_idle_relaunch(W):
         sv.submit(6, W.F[6], update_coords=False)
         assert len(sv.drain()) == 1
         assert sv.launches() >= 2
+
+
+def test_server_placements_match_clustered_batch(lib_path):
+    """The serving kernel solves every RVE on one CTA (all state in shared
+    memory at 1,000 nodes, node state at 5,000, displacements only at 8,000,
+    global memory at 12,000) while a batch run splits the larger ones over
+    clusters of 2 to 8 CTAs: the ramped stress is the same bits either way
+    (same per-fiber and per-node arithmetic, and dt is a minimum)."""
+    import mumfim_gb300 as m
+    from mumfim_gb300 import synthetic as S
+    from mumfim_gb300.serving import RVEServer
+    sizes = (1_000, 5_000, 8_000, 12_000)
+    nets, F = [], []
+    for i, n in enumerate(sizes):
+        coords, conn = S.knn_network(n, 4, S.geometry_seed(8, i))
+        nets.append(m.FiberNetwork(coords, conn, [S._linear_params(8, i)]))
+        F.append(np.eye(3) + (S.uniform(S.param_seed(8, i), 9) * 0.1 - 0.05).reshape(3, 3))
+    w = S.Workload("server placements", nets, [m.SolutionStrategy.ramp(600, 0.5) for _ in nets],
+                   np.stack(F), 600)
+    ref = _batch_sigma(m, w, "mixed")
+    with RVEServer(w.networks, w.strategies, precision="mixed") as sv:
+        for r in range(w.n_rve):
+            sv.submit(r, w.F[r], update_coords=False)
+        res = sv.drain()
+    assert len(res) == w.n_rve
+    for rec in res:
+        assert rec["status"] == 0
+        np.testing.assert_array_equal(rec["sigma"], ref[rec["rve"]])
