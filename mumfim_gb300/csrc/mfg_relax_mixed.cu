@@ -61,11 +61,11 @@ struct MixedState {
   // order[bucket_off[q] .. bucket_off[q + 1]).
   int32_t* order = nullptr;
   int32_t* queues = nullptr;  // one claim counter per bucket
-  int bucket_off[6] = {0, 0, 0, 0, 0, 0};
-  int bucket_grid[5] = {0, 0, 0, 0, 0};
-  cudaStream_t side[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  int bucket_off[7] = {};
+  int bucket_grid[6] = {};
+  cudaStream_t side[6] = {};
   cudaEvent_t fork = nullptr;
-  cudaEvent_t join[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t join[6] = {};
 };
 
 namespace {
@@ -77,8 +77,9 @@ struct BucketKind {
   int cl;    // CTAs per cluster
   bool all;  // fiber force vectors in shared memory too
 };
-constexpr int kBuckets = 5;
-constexpr BucketKind kBucket[kBuckets] = {{8, false}, {4, false}, {4, true}, {2, true}, {1, true}};
+constexpr int kBuckets = 6;
+constexpr BucketKind kBucket[kBuckets] = {{8, false}, {4, false}, {4, true},
+                                          {2, true},  {1, true},  {1, false}};
 
 __global__ void mixed_prepare_kernel(const DevBatch b, MixedState ms) {
   const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
@@ -366,8 +367,10 @@ __device__ __forceinline__ void gather(const Rve& r, const Forces& fv, int i, fl
 // itself; the Green strain follows from du (g l0^2 = du.(dX + du/2)), which
 // keeps its relative precision at small strain where 0.5(l^2/l0^2 - 1)
 // would cancel.
+// Returns the current length l0 sqrt(1 + 2g), which the critical time step
+// needs every 100 steps (unused, and so not computed, on the other steps).
 template <class Nodes>
-__device__ __forceinline__ void fiber_force(const Rve& r, const Nodes& u, int e) {
+__device__ __forceinline__ float fiber_force(const Rve& r, const Nodes& u, int e) {
   const int2 c = __ldg(r.conn + e);
   float ah[3], al[3], bh[3], bl[3];
   u.load(c.x, ah, al);
@@ -386,24 +389,7 @@ __device__ __forceinline__ void fiber_force(const Rve& r, const Nodes& u, int e)
   const float t = tension_over_length(r.L, g, fc.w);
   r.n[e - r.e_base] =
       make_float4((fc.x + du[0]) * t, (fc.y + du[1]) * t, (fc.z + du[2]) * t, 0.f);
-}
-
-// FP64 length of one fiber in the current configuration.
-template <class Nodes>
-__device__ __forceinline__ double length64(const Rve& r, const Nodes& u, const double* X, int e) {
-  const int2 c = __ldg(r.conn + e);
-  float ah[3], al[3], bh[3], bl[3];
-  u.load(c.x, ah, al);
-  u.load(c.y, bh, bl);
-  double s2 = 0.0;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const double* Xk = X + k * r.nt + r.node_off;
-    const double a = Xk[c.x] + (static_cast<double>(ah[k]) + al[k]);
-    const double bq = Xk[c.y] + (static_cast<double>(bh[k]) + bl[k]);
-    s2 += (bq - a) * (bq - a);
-  }
-  return sqrt(s2);
+  return sqrtf(fmaxf(fmaf(2.f, g, 1.f), 0.f)) / fc.w;
 }
 
 // Shared-memory floats of an RVE solved by a cluster of CL CTAs: 9 per node
@@ -423,9 +409,10 @@ __host__ __device__ inline int64_t cluster_floats(int n_nodes, int n_free, int n
 // sorted, so a range is a compact region of the RVE) with their displacement
 // and velocity in its shared memory, and a range of fiber slots whose force
 // vectors it computes: in its shared memory when kAll, else in global memory.
-// A single CTA places the RVE by its size: everything in shared memory,
-// the node state only, the displacements only, or everything in global
-// memory.
+// A single CTA with kAll keeps everything in shared memory (the caller
+// guarantees it fits, so every shared access compiles as one); without kAll
+// it places the RVE by its size: everything in shared memory, the node state
+// only, the displacements only, or everything in global memory.
 template <int CL, bool kAll>
 __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const RunArgs& a, int rve,
                                 double* red, double* cred, float* smem, int smem_floats) {
@@ -479,7 +466,7 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
     vel.set(nodes + 6 * cap, cap);
   } else {
     // force vectors first (16-byte aligned), then the node fields
-    if (cluster_floats(N, NF, E, 1, true) <= smem_floats) {
+    if (kAll || cluster_floats(N, NF, E, 1, true) <= smem_floats) {
       r.n = reinterpret_cast<float4*>(smem);
       own.h.set(smem + 4 * E, N);
       own.l.set(smem + 4 * E + 3 * N, N);
@@ -562,11 +549,10 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
     }
   }
   Ops::sync();
-  double lmin = DBL_MAX;
-  for (int e = e_lo + tid; e < e_hi; e += kThreadsMixed) {
-    fiber_force(r, u, e);
-    lmin = fmin(lmin, length64(r, u, b.X, e));
-  }
+  // critical step from the shortest current fiber (FP32 length from the
+  // Green strain, ~1e-7 relative; h itself is an FP32 number)
+  float lmin = FLT_MAX;
+  for (int e = e_lo + tid; e < e_hi; e += kThreadsMixed) lmin = fminf(lmin, fiber_force(r, u, e));
   double dt_crit =
       Ops::template combine<true>(block_min<kThreadsMixed>(lmin, red), cred) / d.sound_speed;
 
@@ -633,11 +619,8 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
     Ops::sync();
     const bool dt_step = (step % kUpdateFreq) == 0;
     if (dt_step) {
-      double lm = DBL_MAX;
-      for (int e = e_lo + tid; e < e_hi; e += kThreadsMixed) {
-        fiber_force(r, u, e);
-        lm = fmin(lm, length64(r, u, b.X, e));
-      }
+      float lm = FLT_MAX;
+      for (int e = e_lo + tid; e < e_hi; e += kThreadsMixed) lm = fminf(lm, fiber_force(r, u, e));
       dt_crit =
           Ops::template combine<true>(block_min<kThreadsMixed>(lm, red), cred) / d.sound_speed;
       h_cur = static_cast<float>(d.crit * dt_crit * 0.5);
@@ -750,7 +733,7 @@ server_mixed_kernel(const DevBatch b, const MixedState ms, const ServerArgs sa, 
   __shared__ double red[kThreadsMixed / 32 + 1];
   __shared__ double cred[1];
   server_loop(sa, [&](const RunArgs& a, int rve) {
-    solve_rve_mixed<1, true>(b, ms, a, rve, red, cred, smem, smem_floats);
+    solve_rve_mixed<1, false>(b, ms, a, rve, red, cred, smem, smem_floats);
   });
 }
 
@@ -892,7 +875,8 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
       case 1: e = setup_bucket<kBucket[1].cl, kBucket[1].all>(ms, n, q); break;
       case 2: e = setup_bucket<kBucket[2].cl, kBucket[2].all>(ms, n, q); break;
       case 3: e = setup_bucket<kBucket[3].cl, kBucket[3].all>(ms, n, q); break;
-      default: e = setup_bucket<kBucket[4].cl, kBucket[4].all>(ms, n, q); break;
+      case 4: e = setup_bucket<kBucket[4].cl, kBucket[4].all>(ms, n, q); break;
+      default: e = setup_bucket<kBucket[5].cl, kBucket[5].all>(ms, n, q); break;
     }
     if (e != cudaSuccess) return e;
     if ((e = cudaStreamCreateWithFlags(&ms.side[q], cudaStreamNonBlocking)) != cudaSuccess)
@@ -939,7 +923,8 @@ cudaError_t run_mixed(MixedState& ms, const DevBatch& b, const RunArgs& a, cudaS
       case 1: e = launch_bucket<kBucket[1].cl, kBucket[1].all>(ms, b, a, q, sq); break;
       case 2: e = launch_bucket<kBucket[2].cl, kBucket[2].all>(ms, b, a, q, sq); break;
       case 3: e = launch_bucket<kBucket[3].cl, kBucket[3].all>(ms, b, a, q, sq); break;
-      default: e = launch_bucket<kBucket[4].cl, kBucket[4].all>(ms, b, a, q, sq); break;
+      case 4: e = launch_bucket<kBucket[4].cl, kBucket[4].all>(ms, b, a, q, sq); break;
+      default: e = launch_bucket<kBucket[5].cl, kBucket[5].all>(ms, b, a, q, sq); break;
     }
     if (e != cudaSuccess) return e;
     ++*launches;
