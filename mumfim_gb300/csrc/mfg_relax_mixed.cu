@@ -331,10 +331,9 @@ struct ClusterOps {
 // Nodal internal force: incident fiber vectors in the node's CSR order,
 // subtracted at a fiber's first end and added at its second.
 template <class Forces>
-__device__ __forceinline__ void gather(const Rve& r, const Forces& fv, int i, float& a0, float& a1,
-                                       float& a2) {
+__device__ __forceinline__ void gather_row(const Rve& r, const Forces& fv, int pb, int pe, float& a0,
+                                           float& a1, float& a2) {
   a0 = 0.f; a1 = 0.f; a2 = 0.f;
-  const int pb = __ldg(r.rowptr + i), pe = __ldg(r.rowptr + i + 1);
   int p = pb;
   // four incidences in flight, summed in CSR order
   for (; p + 4 <= pe; p += 4) {
@@ -362,6 +361,29 @@ __device__ __forceinline__ void gather(const Rve& r, const Forces& fv, int i, fl
   }
 }
 
+template <class Forces>
+__device__ __forceinline__ void gather(const Rve& r, const Forces& fv, int i, float& a0, float& a1,
+                                       float& a2) {
+  gather_row(r, fv, __ldg(r.rowptr + i), __ldg(r.rowptr + i + 1), a0, a1, a2);
+}
+
+// Read-only data of one fiber (end nodes; dX and 1/l0) and of one node (CSR
+// row bounds; 1/m and m), loaded one item ahead of its use in the passes.
+struct FiberConst {
+  int2 c;
+  float4 fc;
+};
+struct NodeConst {
+  int pb, pe;
+  float2 mm;
+};
+__device__ __forceinline__ FiberConst load_fiber(const Rve& r, int e) {
+  return {__ldg(r.conn + e), __ldg(r.fcon + e)};
+}
+__device__ __forceinline__ NodeConst load_node(const Rve& r, int i) {
+  return {__ldg(r.rowptr + i), __ldg(r.rowptr + i + 1), __ldg(r.mass + i)};
+}
+
 // Force vector of one fiber. The displacement difference du is formed with a
 // TwoSum of the hi parts plus the lo parts, so it is accurate to FP32 of du
 // itself; the Green strain follows from du (g l0^2 = du.(dX + du/2)), which
@@ -370,8 +392,9 @@ __device__ __forceinline__ void gather(const Rve& r, const Forces& fv, int i, fl
 // Returns the current length l0 sqrt(1 + 2g), which the critical time step
 // needs every 100 steps (unused, and so not computed, on the other steps).
 template <class Nodes>
-__device__ __forceinline__ float fiber_force(const Rve& r, const Nodes& u, int e) {
-  const int2 c = __ldg(r.conn + e);
+__device__ __forceinline__ float fiber_force(const Rve& r, const Nodes& u, int e,
+                                             const FiberConst& k) {
+  const int2 c = k.c;
   float ah[3], al[3], bh[3], bl[3];
   u.load(c.x, ah, al);
   u.load(c.y, bh, bl);
@@ -382,7 +405,7 @@ __device__ __forceinline__ float fiber_force(const Rve& r, const Nodes& u, int e
     two_sum(bh[k], -ah[k], d, ed);
     du[k] = d + (ed + (bl[k] - al[k]));
   }
-  const float4 fc = __ldg(r.fcon + e);
+  const float4 fc = k.fc;
   const float gn = fmaf(du[0], fmaf(0.5f, du[0], fc.x),
                         fmaf(du[1], fmaf(0.5f, du[1], fc.y), du[2] * fmaf(0.5f, du[2], fc.z)));
   const float g = gn * (fc.w * fc.w);
@@ -390,6 +413,29 @@ __device__ __forceinline__ float fiber_force(const Rve& r, const Nodes& u, int e
   r.n[e - r.e_base] =
       make_float4((fc.x + du[0]) * t, (fc.y + du[1]) * t, (fc.z + du[2]) * t, 0.f);
   return sqrtf(fmaxf(fmaf(2.f, g, 1.f), 0.f)) / fc.w;
+}
+
+// Force vectors of fiber slots e_lo + tid, + kThreadsMixed, ... < e_hi, the
+// next slot's read-only data loaded while the current one is computed.
+// Returns the shortest current length among them when kLen.
+template <bool kLen, class Nodes>
+__device__ __forceinline__ float fiber_pass(const Rve& r, const Nodes& u, int e_lo, int e_hi) {
+  float lmin = FLT_MAX;
+  int e = e_lo + static_cast<int>(threadIdx.x);
+  if (e >= e_hi) return lmin;
+  FiberConst cur = load_fiber(r, e);
+  for (;;) {
+    const int en = e + kThreadsMixed;
+    const bool more = en < e_hi;
+    FiberConst nxt = cur;
+    if (more) nxt = load_fiber(r, en);
+    const float l = fiber_force(r, u, e, cur);
+    if (kLen) lmin = fminf(lmin, l);
+    if (!more) break;
+    cur = nxt;
+    e = en;
+  }
+  return lmin;
 }
 
 // Shared-memory floats of an RVE solved by a cluster of CL CTAs: 9 per node
@@ -551,8 +597,7 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   Ops::sync();
   // critical step from the shortest current fiber (FP32 length from the
   // Green strain, ~1e-7 relative; h itself is an FP32 number)
-  float lmin = FLT_MAX;
-  for (int e = e_lo + tid; e < e_hi; e += kThreadsMixed) lmin = fminf(lmin, fiber_force(r, u, e));
+  const float lmin = fiber_pass<true>(r, u, e_lo, e_hi);
   double dt_crit =
       Ops::template combine<true>(block_min<kThreadsMixed>(lmin, red), cred) / d.sound_speed;
 
@@ -585,22 +630,34 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
     const float h = h_cur;
     const float hk = h_prev + h;  // trailing kick of step-1 + leading kick of step
     const float h2 = h + h;
-    for (int i = f_lo + tid; i < f_hi; i += kThreadsMixed) {
-      float f[3];
-      gather(r, fv, i, f[0], f[1], f[2]);
-      const float2 mm = __ldg(r.mass + i);
-      const float mc = mm.y * c;
-      const float km = hk * mm.x;
-      const int li = i - f_lo;
+    // node pass over the own free nodes, the next node's row bounds and mass
+    // loaded while the current one is gathered
+    if (f_lo + tid < f_hi) {
+      int i = f_lo + tid;
+      NodeConst cur = load_node(r, i);
+      for (;;) {
+        const int in = i + kThreadsMixed;
+        const bool more = in < f_hi;
+        NodeConst nxt = cur;
+        if (more) nxt = load_node(r, in);
+        float f[3];
+        gather_row(r, fv, cur.pb, cur.pe, f[0], f[1], f[2]);
+        const float mc = cur.mm.y * c;
+        const float km = hk * cur.mm.x;
+        const int li = i - f_lo;
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        float w = vel(k, li);
-        w = fmaf(km, -f[k] - mc * w, w);
-        vel(k, li) = w;
-        float hi = own.hi(k, li), lo = own.lo(k, li);
-        comp_add(hi, lo, h2 * w);
-        own.hi(k, li) = hi;
-        own.lo(k, li) = lo;
+        for (int k = 0; k < 3; ++k) {
+          float w = vel(k, li);
+          w = fmaf(km, -f[k] - mc * w, w);
+          vel(k, li) = w;
+          float hi = own.hi(k, li), lo = own.lo(k, li);
+          comp_add(hi, lo, h2 * w);
+          own.hi(k, li) = hi;
+          own.lo(k, li) = lo;
+        }
+        if (!more) break;
+        cur = nxt;
+        i = in;
       }
     }
     if (ramp) {
@@ -619,18 +676,12 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
     Ops::sync();
     const bool dt_step = (step % kUpdateFreq) == 0;
     if (dt_step) {
-      float lm = FLT_MAX;
-      for (int e = e_lo + tid; e < e_hi; e += kThreadsMixed) lm = fminf(lm, fiber_force(r, u, e));
+      const float lm = fiber_pass<true>(r, u, e_lo, e_hi);
       dt_crit =
           Ops::template combine<true>(block_min<kThreadsMixed>(lm, red), cred) / d.sound_speed;
       h_cur = static_cast<float>(d.crit * dt_crit * 0.5);
     } else {
-      int e = e_lo + tid;
-      for (; e + kThreadsMixed < e_hi; e += 2 * kThreadsMixed) {
-        fiber_force(r, u, e);
-        fiber_force(r, u, e + kThreadsMixed);
-      }
-      if (e < e_hi) fiber_force(r, u, e);
+      fiber_pass<false>(r, u, e_lo, e_hi);
       Ops::sync();
     }
     h_prev = h;
