@@ -878,7 +878,7 @@ struct PendingReq {
 // working set when used), for admission against the HBM budget.
 double batch_bytes(int64_t nt, int64_t et, int64_t nbt, int64_t R, bool mixed) {
   double b = nt * (5 * 3 * 8.0 + 8 + 4) + et * (8.0 + 8 + 24 + 8) + nbt * (48.0 + 4) + R * 200.0;
-  if (mixed) b += nt * (24.0 + 16 + 8) + et * (16.0 + 16);
+  if (mixed) b += nt * (24.0 + 12 + 8) + et * (16.0 + 16 + 8 + 8) + R * 8.0;
   return b;
 }
 

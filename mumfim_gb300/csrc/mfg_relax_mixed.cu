@@ -48,12 +48,18 @@ namespace cg = cooperative_groups;
 namespace mfg {
 
 struct MixedState {
-  float* u_hi = nullptr;   // 3 * nt (STREAM placement)
-  float* u_lo = nullptr;   // 3 * nt
-  float* v = nullptr;      // 3 * nt, velocity (STREAM placement)
+  float* u_hl = nullptr;   // 6 * nt, node records (hi x, y, z, lo x, y, z); STREAM placement
+  float* v = nullptr;      // 3 * nt, velocity (x, y, z per node); placements without it on chip
   float2* mass = nullptr;  // nt, (1 / m, m)
   float4* fcon = nullptr;  // et, (X[n2] - X[n1], 1 / l0) rounded to FP32
   float4* nrm = nullptr;   // et, per-fiber force vectors (scratch; w unused)
+  // Where a cluster-solved RVE keeps what its passes read: per fiber slot the
+  // two end nodes as (owner CTA << 24 | local record), per CSR incidence the
+  // force vector as (owner CTA << 24 | local slot << 1 | end). Single-CTA
+  // RVEs use the plain node ids and incidence codes of the batch.
+  int2* econn = nullptr;      // et
+  int32_t* icode = nullptr;   // 2 * et
+  int32_t* rve_part = nullptr;  // per RVE: cluster size | (force vectors on chip) << 8
   int sms = 1;
   int smem_bytes = 0;
   // Size buckets of the batch run (kBucket[q]: cluster size, force vectors
@@ -102,6 +108,36 @@ __global__ void mixed_prepare_fibers_kernel(const DevBatch b, MixedState ms) {
       dx[k] = static_cast<float>(X[c.y] - X[c.x]);
     }
     ms.fcon[fo] = make_float4(dx[0], dx[1], dx[2], static_cast<float>(1.0 / b.l0[fo]));
+    const int part = ms.rve_part[rve];
+    const int cl = part & 0xFF;
+    if (cl > 1) {
+      // node j -> (owner, record): free and boundary nodes are split
+      // separately into cl blocks (the layout solve_rve_mixed uses)
+      const int NF = d.n_free, NB = d.n_nodes - d.n_free;
+      const int fchunk = (NF + cl - 1) / cl, bchunk = (NB + cl - 1) / cl;
+      auto code = [&](int j) {
+        int o, local;
+        if (j < NF) {
+          o = j / fchunk;
+          local = j - o * fchunk;
+        } else {
+          o = (j - NF) / bchunk;
+          local = fchunk + (j - NF) - o * bchunk;
+        }
+        return (o << 24) | local;
+      };
+      ms.econn[fo] = make_int2(code(c.x), code(c.y));
+      if (part >> 8) {
+        const int echunk = (d.n_fibers + cl - 1) / cl;
+        for (int q = 0; q < 2; ++q) {
+          const int64_t pi = d.inc_off + 2 * static_cast<int64_t>(e) + q;
+          const int ic = b.inc[pi];
+          const int slot = ic >> 1;
+          const int o = slot / echunk;
+          ms.icode[pi] = (o << 24) | ((slot - o * echunk) << 1) | (ic & 1);
+        }
+      }
+    }
   }
 }
 
@@ -178,17 +214,6 @@ __device__ __forceinline__ void split(double u, float& hi, float& lo) {
   lo = static_cast<float>(u - static_cast<double>(hi));
 }
 
-// A three-component float field: component k of node i at c[k][i].
-struct Field3 {
-  float* c[3];
-  __device__ __forceinline__ void set(float* base, int64_t stride) {
-    c[0] = base;
-    c[1] = base + stride;
-    c[2] = base + 2 * stride;
-  }
-  __device__ __forceinline__ float& operator()(int k, int i) const { return c[k][i]; }
-};
-
 struct Rve {
   RveDesc d;
   Law L;
@@ -196,94 +221,81 @@ struct Rve {
   int e_base;
   const float2* mass;   // (1 / m, m)
   const float4* fcon;   // (dX, 1 / l0)
-  const int2* conn;
+  const int2* conn;     // end nodes (node ids, or cluster codes)
   const int32_t* rowptr;
-  const int32_t* inc;
+  const int32_t* inc;   // incidences (slot << 1 | end, or cluster codes)
   float* ramp;          // per boundary node: step increment d/n as (hi[3], lo[3])
   int64_t node_off, nt;
 };
 
-// Owner of element j of a field split into CL blocks of `chunk`.
-template <int CL>
-__device__ __forceinline__ int owner(int j, int chunk) {
-  int o = 0;
-#pragma unroll
-  for (int q = 1; q < CL; ++q) o += (j >= q * chunk) ? 1 : 0;
-  return o;
-}
-
 // Shared-window address of `local` in CTA `o` of this cluster.
-__device__ __forceinline__ uint32_t cluster_addr(uint32_t local, int o) {
+__device__ __forceinline__ uint32_t cluster_addr(uint32_t local, uint32_t o) {
   uint32_t remote;
   asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(local), "r"(o));
   return remote;
 }
 
-// Node displacement (hi, lo) of an RVE solved by one CTA: in its shared
-// memory (resident placements) or in global memory (streaming placement).
-// Also the view a CTA of a cluster has of the nodes it owns, by local index.
+// A node record: displacement hi x, y, z then lo x, y, z, six floats read
+// and written as three 8-byte pairs.
+struct NodeRec {
+  float hi[3], lo[3];
+};
+__device__ __forceinline__ NodeRec load_rec(const float* rec) {
+  const float2* p = reinterpret_cast<const float2*>(rec);
+  const float2 a = p[0], b = p[1], c = p[2];
+  return {{a.x, a.y, b.x}, {b.y, c.x, c.y}};
+}
+__device__ __forceinline__ void store_rec(float* rec, const NodeRec& r) {
+  float2* p = reinterpret_cast<float2*>(rec);
+  p[0] = make_float2(r.hi[0], r.hi[1]);
+  p[1] = make_float2(r.hi[2], r.lo[0]);
+  p[2] = make_float2(r.lo[1], r.lo[2]);
+}
+
+// Node records of an RVE solved by one CTA (shared or global memory), by
+// node id; also a cluster CTA's view of its own nodes, by local record.
 struct LocalNodes {
-  Field3 h, l;
-  __device__ __forceinline__ float& hi(int k, int j) const { return h(k, j); }
-  __device__ __forceinline__ float& lo(int k, int j) const { return l(k, j); }
-  __device__ __forceinline__ void load(int j, float (&uh)[3], float (&ul)[3]) const {
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      uh[k] = h(k, j);
-      ul[k] = l(k, j);
-    }
-  }
+  float* hl;
+  __device__ __forceinline__ NodeRec load(int j) const { return load_rec(hl + 6 * j); }
+  __device__ __forceinline__ float* rec(int j) const { return hl + 6 * j; }
 };
 
-// Node displacement of an RVE split over the CL CTAs of a thread-block
-// cluster, read through distributed shared memory. The free nodes [0, nf)
-// and the boundary nodes [nf, N) are split separately into CL contiguous
-// blocks of fchunk and bchunk (both segments are Morton-sorted, so CTA o gets
-// the free and the boundary nodes of the same region of the RVE). CTA o keeps
-// its free nodes at local index 0.. and its boundary nodes at fchunk.., in six
-// component arrays of `cap` floats (hi x, y, z, lo x, y, z) at the same
-// shared-memory offset `base` in every CTA.
+// Node records of an RVE split over the CTAs of a cluster, read through
+// distributed shared memory. CTA o owns a contiguous block of the free nodes
+// and one of the boundary nodes (both segments are Morton-sorted, so the two
+// blocks cover the same region of the RVE) and keeps their records at the
+// same shared-memory offset `base` in every CTA; an end node is given by its
+// code (owner << 24 | record).
 template <int CL>
 struct ClusterNodes {
-  uint32_t base;  // shared-window address of this CTA's block
-  int fchunk, bchunk, nf, cap;
-  __device__ __forceinline__ void load(int j, float (&uh)[3], float (&ul)[3]) const {
-    int o, local;
-    if (j < nf) {
-      o = owner<CL>(j, fchunk);
-      local = j - o * fchunk;
-    } else {
-      const int jb = j - nf;
-      o = owner<CL>(jb, bchunk);
-      local = fchunk + jb - o * bchunk;
-    }
-    const uint32_t remote = cluster_addr(base + 4u * static_cast<uint32_t>(local), o);
-    const uint32_t stride = 4u * static_cast<uint32_t>(cap);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(uh[k]) : "r"(remote + k * stride));
-      asm volatile("ld.shared::cluster.f32 %0, [%1];"
-                   : "=f"(ul[k])
-                   : "r"(remote + (3 + k) * stride));
-    }
+  uint32_t base;
+  __device__ __forceinline__ NodeRec load(int code) const {
+    const uint32_t o = static_cast<uint32_t>(code) >> 24;
+    const uint32_t a = cluster_addr(base + 24u * (static_cast<uint32_t>(code) & 0xFFFFFFu), o);
+    float2 p0, p1, p2;
+    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(p0.x), "=f"(p0.y) : "r"(a));
+    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(p1.x), "=f"(p1.y) : "r"(a + 8));
+    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(p2.x), "=f"(p2.y) : "r"(a + 16));
+    return {{p0.x, p0.y, p1.x}, {p1.y, p2.x, p2.y}};
   }
 };
 
-// Fiber force vectors in one CTA's shared memory or in global memory.
+// Fiber force vectors in one CTA's shared memory or in global memory, by
+// incidence code (slot << 1 | end).
 struct LocalForces {
   const float4* p;
-  __device__ __forceinline__ float4 load(int e) const { return p[e]; }
+  __device__ __forceinline__ float4 load(int code) const { return p[code >> 1]; }
 };
 
-// Fiber force vectors of an RVE split over a cluster: CTA o holds slots
-// [o*echunk, (o+1)*echunk) as float4 at shared-memory offset 0.
+// Fiber force vectors of an RVE split over a cluster: CTA o holds its slots
+// as float4 at shared-memory offset 0; an incidence is given by its code
+// (owner << 24 | local slot << 1 | end).
 template <int CL>
 struct ClusterForces {
   uint32_t base;
-  int echunk;
-  __device__ __forceinline__ float4 load(int e) const {
-    const int o = owner<CL>(e, echunk);
-    const uint32_t a = cluster_addr(base + 16u * static_cast<uint32_t>(e - o * echunk), o);
+  __device__ __forceinline__ float4 load(int code) const {
+    const uint32_t o = static_cast<uint32_t>(code) >> 24;
+    const uint32_t a = cluster_addr(base + 8u * (static_cast<uint32_t>(code) & 0xFFFFFEu), o);
     float4 t;
     asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
                  : "=f"(t.x), "=f"(t.y), "=f"(t.z), "=f"(t.w)
@@ -342,7 +354,7 @@ __device__ __forceinline__ void gather_row(const Rve& r, const Forces& fv, int p
 #pragma unroll
     for (int q = 0; q < 4; ++q) code[q] = __ldg(r.inc + p + q);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) t[q] = fv.load(code[q] >> 1);
+    for (int q = 0; q < 4; ++q) t[q] = fv.load(code[q]);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const float sg = (code[q] & 1) ? 1.f : -1.f;
@@ -353,7 +365,7 @@ __device__ __forceinline__ void gather_row(const Rve& r, const Forces& fv, int p
   }
   for (; p < pe; ++p) {
     const int code = __ldg(r.inc + p);
-    const float4 t = fv.load(code >> 1);
+    const float4 t = fv.load(code);
     const float sg = (code & 1) ? 1.f : -1.f;
     a0 = fmaf(sg, t.x, a0);
     a1 = fmaf(sg, t.y, a1);
@@ -394,16 +406,13 @@ __device__ __forceinline__ NodeConst load_node(const Rve& r, int i) {
 template <class Nodes>
 __device__ __forceinline__ float fiber_force(const Rve& r, const Nodes& u, int e,
                                              const FiberConst& k) {
-  const int2 c = k.c;
-  float ah[3], al[3], bh[3], bl[3];
-  u.load(c.x, ah, al);
-  u.load(c.y, bh, bl);
+  const NodeRec na = u.load(k.c.x), nb = u.load(k.c.y);
   float du[3];
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
+  for (int q = 0; q < 3; ++q) {
     float d, ed;
-    two_sum(bh[k], -ah[k], d, ed);
-    du[k] = d + (ed + (bl[k] - al[k]));
+    two_sum(nb.hi[q], -na.hi[q], d, ed);
+    du[q] = d + (ed + (nb.lo[q] - na.lo[q]));
   }
   const float4 fc = k.fc;
   const float gn = fmaf(du[0], fmaf(0.5f, du[0], fc.x),
@@ -486,61 +495,54 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   using Nodes = std::conditional_t<(CL > 1), ClusterNodes<CL>, LocalNodes>;
   using Forces = std::conditional_t<(CL > 1 && kAll), ClusterForces<CL>, LocalForces>;
   Nodes u;         // every node of the RVE (fiber pass)
-  LocalNodes own;  // the nodes this CTA updates, by local index
-  Field3 vel;      // their velocities, by local index
+  LocalNodes own;  // the node records this CTA updates, by local index
+  float* vel;      // their velocities (x, y, z), by local index
   Forces fv;       // every fiber force vector of the RVE (node pass)
   r.e_base = 0;
+  r.conn = b.conn + fo;
+  r.inc = b.inc + d.inc_off;
   if constexpr (CL > 1) {
     float* nodes = smem;
+    r.conn = ms.econn + fo;
     if constexpr (kAll) {
       r.n = reinterpret_cast<float4*>(smem);
       r.e_base = e_lo;
+      r.inc = ms.icode + d.inc_off;
       fv.base = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
-      fv.echunk = echunk;
       nodes = smem + 4 * echunk;
     } else {
       r.n = ms.nrm + fo;
       fv.p = r.n;
     }
     u.base = static_cast<uint32_t>(__cvta_generic_to_shared(nodes));
-    u.fchunk = fchunk;
-    u.bchunk = bchunk;
-    u.nf = NF;
-    u.cap = cap;
-    own.h.set(nodes, cap);
-    own.l.set(nodes + 3 * cap, cap);
-    vel.set(nodes + 6 * cap, cap);
+    own.hl = nodes;
+    vel = nodes + 6 * cap;
   } else {
-    // force vectors first (16-byte aligned), then the node fields
+    // force vectors first (16-byte aligned), then the node records, then the
+    // velocities
     if (kAll || cluster_floats(N, NF, E, 1, true) <= smem_floats) {
       r.n = reinterpret_cast<float4*>(smem);
-      own.h.set(smem + 4 * E, N);
-      own.l.set(smem + 4 * E + 3 * N, N);
-      vel.set(smem + 4 * E + 6 * N, N);
+      own.hl = smem + 4 * E;
+      vel = smem + 4 * E + 6 * N;
     } else if (cluster_floats(N, NF, E, 1, false) <= smem_floats) {
       r.n = ms.nrm + fo;
-      own.h.set(smem, N);
-      own.l.set(smem + 3 * N, N);
-      vel.set(smem + 6 * N, N);
+      own.hl = smem;
+      vel = smem + 6 * N;
     } else if (6LL * N <= smem_floats) {
       r.n = ms.nrm + fo;
-      own.h.set(smem, N);
-      own.l.set(smem + 3 * N, N);
-      vel.set(ms.v + no, nt);
+      own.hl = smem;
+      vel = ms.v + 3 * no;
     } else {
       r.n = ms.nrm + fo;
-      own.h.set(ms.u_hi + no, nt);
-      own.l.set(ms.u_lo + no, nt);
-      vel.set(ms.v + no, nt);
+      own.hl = ms.u_hl + 6 * no;
+      vel = ms.v + 3 * no;
     }
     fv.p = r.n;
     u = own;
   }
   r.mass = ms.mass + no;
   r.fcon = ms.fcon + fo;
-  r.conn = b.conn + fo;
   r.rowptr = b.rowptr + d.row_off;
-  r.inc = b.inc + d.inc_off;
   r.ramp = reinterpret_cast<float*>(b.ramp + 6 * d.bnd_off);  // 12 floats per boundary node
   const double* F = a.F + 9 * (a.n_F > 1 ? rve : 0);
   const bool ramp = d.mode == 1;
@@ -567,15 +569,14 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
       up[0] = u0; up[1] = u1; up[2] = u2;
     }
     double xn[3];
+    NodeRec nr;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       xn[k] = X[k] + up[k];
-      float hi, lo;
-      split(xn[k] - X[k], hi, lo);
-      own.hi(k, li) = hi;
-      own.lo(k, li) = lo;
-      vel(k, li) = 0.f;
+      split(xn[k] - X[k], nr.hi[k], nr.lo[k]);
+      vel[3 * li + k] = 0.f;
     }
+    store_rec(own.rec(li), nr);
     if (ramp && i >= NF) {
       // The boundary moves by d/n per step, d = (F - I) x0. The increment is
       // kept as an exact FP32 pair and accumulated without rounding into
@@ -645,16 +646,16 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
         const float mc = cur.mm.y * c;
         const float km = hk * cur.mm.x;
         const int li = i - f_lo;
+        float* rec = own.rec(li);
+        NodeRec nr = load_rec(rec);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-          float w = vel(k, li);
+          float w = vel[3 * li + k];
           w = fmaf(km, -f[k] - mc * w, w);
-          vel(k, li) = w;
-          float hi = own.hi(k, li), lo = own.lo(k, li);
-          comp_add(hi, lo, h2 * w);
-          own.hi(k, li) = hi;
-          own.lo(k, li) = lo;
+          vel[3 * li + k] = w;
+          comp_add(nr.hi[k], nr.lo[k], h2 * w);
         }
+        store_rec(rec, nr);
         if (!more) break;
         cur = nxt;
         i = in;
@@ -663,14 +664,16 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
     if (ramp) {
       for (int i = g_lo + tid; i < g_hi; i += kThreadsMixed) {
         const float* rb = r.ramp + 12 * (i - NF);
-        const int li = fchunk + (i - g_lo);
+        float* rec = own.rec(fchunk + (i - g_lo));
+        NodeRec nr = load_rec(rec);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
           float s, e;
-          two_sum(own.hi(k, li), rb[k], s, e);
-          own.hi(k, li) = s;
-          own.lo(k, li) = own.lo(k, li) + (e + rb[3 + k]);
+          two_sum(nr.hi[k], rb[k], s, e);
+          nr.hi[k] = s;
+          nr.lo[k] = nr.lo[k] + (e + rb[3 + k]);
         }
+        store_rec(rec, nr);
       }
     }
     Ops::sync();
@@ -693,10 +696,11 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   for (int t = tid; t < n_own; t += kThreadsMixed) {
     const int i = t < nfo ? f_lo + t : g_lo + (t - nfo);
     const int li = t < nfo ? t : fchunk + (t - nfo);
+    const NodeRec nr = load_rec(own.rec(li));
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       const double Xk = b.X[k * nt + no + i];
-      const double xk = Xk + (static_cast<double>(own.hi(k, li)) + own.lo(k, li));
+      const double xk = Xk + (static_cast<double>(nr.hi[k]) + nr.lo[k]);
       b.x[k * nt + no + i] = xk;
       if (a.update_coords) b.u[k * nt + no + i] = xk - Xk;
     }
@@ -799,7 +803,8 @@ MixedState* mixed_new() { return new MixedState(); }
 
 void mixed_destroy(MixedState* ms) {
   if (!ms) return;
-  for (void* p : {static_cast<void*>(ms->u_hi), static_cast<void*>(ms->u_lo),
+  for (void* p : {static_cast<void*>(ms->u_hl), static_cast<void*>(ms->econn),
+                  static_cast<void*>(ms->icode), static_cast<void*>(ms->rve_part),
                   static_cast<void*>(ms->v), static_cast<void*>(ms->mass),
                   static_cast<void*>(ms->fcon), static_cast<void*>(ms->nrm),
                   static_cast<void*>(ms->order), static_cast<void*>(ms->queues)})
@@ -887,12 +892,14 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
                          int sms, cudaStream_t s) {
   cudaError_t e;
   const size_t nt = static_cast<size_t>(b.nt), et = static_cast<size_t>(b.et);
-  if ((e = alloc(&ms.u_hi, 3 * nt)) != cudaSuccess) return e;
-  if ((e = alloc(&ms.u_lo, 3 * nt)) != cudaSuccess) return e;
+  if ((e = alloc(&ms.u_hl, 6 * nt)) != cudaSuccess) return e;
   if ((e = alloc(&ms.v, 3 * nt)) != cudaSuccess) return e;
   if ((e = alloc(&ms.mass, nt)) != cudaSuccess) return e;
   if ((e = alloc(&ms.fcon, et)) != cudaSuccess) return e;
   if ((e = alloc(&ms.nrm, et)) != cudaSuccess) return e;
+  if ((e = alloc(&ms.econn, et)) != cudaSuccess) return e;
+  if ((e = alloc(&ms.icode, 2 * et)) != cudaSuccess) return e;
+  if ((e = alloc(&ms.rve_part, desc.size())) != cudaSuccess) return e;
   if ((e = alloc(&ms.order, desc.size())) != cudaSuccess) return e;
   if ((e = alloc(&ms.queues, kBuckets)) != cudaSuccess) return e;
   ms.sms = sms;
@@ -904,8 +911,16 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
 
   // size buckets, each in longest-processing-time order
   std::vector<std::vector<int32_t>> bucket(kBuckets);
-  for (size_t r = 0; r < desc.size(); ++r)
-    bucket[bucket_of(desc[r], smem_floats)].push_back(static_cast<int32_t>(r));
+  std::vector<int32_t> part(desc.size());
+  for (size_t r = 0; r < desc.size(); ++r) {
+    const int q = bucket_of(desc[r], smem_floats);
+    bucket[q].push_back(static_cast<int32_t>(r));
+    part[r] = kBucket[q].cl | (kBucket[q].all ? 1 << 8 : 0);
+  }
+  if (!part.empty() &&
+      (e = cudaMemcpy(ms.rve_part, part.data(), part.size() * sizeof(int32_t),
+                      cudaMemcpyHostToDevice)) != cudaSuccess)
+    return e;
   std::vector<int32_t> order;
   order.reserve(desc.size());
   for (int q = 0; q < kBuckets; ++q) {
@@ -916,8 +931,8 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
   }
   ms.bucket_off[kBuckets] = static_cast<int>(order.size());
   if (!order.empty() &&
-      (e = cudaMemcpyAsync(ms.order, order.data(), order.size() * sizeof(int32_t),
-                           cudaMemcpyHostToDevice, s)) != cudaSuccess)
+      (e = cudaMemcpy(ms.order, order.data(), order.size() * sizeof(int32_t),
+                      cudaMemcpyHostToDevice)) != cudaSuccess)
     return e;
   for (int q = 0; q < kBuckets; ++q) {
     const int n = ms.bucket_off[q + 1] - ms.bucket_off[q];
