@@ -199,6 +199,48 @@ size_t mfg_batch_state_bytes(const mfg_batch* batch, int32_t rve);
 mfg_status mfg_batch_export_state(mfg_batch* batch, int32_t rve, void* buf, size_t bytes);
 mfg_status mfg_batch_import_state(mfg_batch* batch, int32_t rve, const void* buf, size_t bytes);
 
+/* ---- multiscale coupling ---------------------------------------------- */
+/* Record sizes of the macro/micro exchange (MultiscaleMicroFOParams.h:79-104):
+ * micro_fo_data = F (9), micro_fo_result = sigma (6) + averaged volume stress
+ * (3, zero as in the reference) + stiffness (36), micro_fo_step_result = 3-D
+ * orientation tensor (9) + 2-D orientation tensor (9), micro_fo_params = the
+ * fiber_param_fields below. */
+#define MFG_MICRO_FO_DATA 9
+#define MFG_MICRO_FO_RESULT 45
+#define MFG_MICRO_FO_STEP_RESULT 18
+enum {
+  MFG_PRM_FIBER_RADIUS = 0,
+  MFG_PRM_VOLUME_FRACTION = 1,
+  MFG_PRM_YOUNGS_MODULUS = 2,
+  MFG_PRM_NONLINEAR_PARAM = 3,
+  MFG_PRM_LINEAR_TRANSITION = 4,
+  MFG_PRM_ORIENTATION_AXIS_X = 5,
+  MFG_PRM_ORIENTATION_AXIS_Y = 6,
+  MFG_PRM_ORIENTATION_AXIS_Z = 7,
+  MFG_MICRO_FO_PARAMS = 8
+};
+/* Replaces calcScaleConversion(mesh, fbr_area, fbr_vol_frc)
+ * (src/mumfim/microscale/MultiscaleCoupling.cc:7-23, called at
+ * MultiscaleRVEAnalysis.cc:159-167): with L the summed reference length of
+ * the fibers and A = pi r^2, the RVE edge is d = sqrt(L A / volume_fraction)
+ * and the factor 1 / d^2 goes into mfg_network.scale_factor. Host only. */
+mfg_status mfg_scale_conversion(int32_t n_nodes, const double* coords, int32_t n_fibers,
+                                const int32_t* connectivity, double fiber_radius,
+                                double volume_fraction, double* factor);
+/* One macro iteration of the batched microscale service
+ * (MultiscaleRVEAnalysis.cc:232-289): data holds n_rve micro_fo_data records
+ * (row-major F), the batch runs with update_coords = 1, the stiffness follows,
+ * and results receives n_rve micro_fo_result records. status may be NULL.
+ * Returns what mfg_batch_run() returns (results are filled either way), or
+ * the stiffness's error. Blocking. */
+mfg_status mfg_batch_micro_fo_iterate(mfg_batch* batch, const double* data, double* results,
+                                      mfg_rve_status* status);
+/* Step results of the service (recoverMultiscaleStepResults,
+ * MultiscaleCoupling.h:46-66): params holds n_rve micro_fo_params records;
+ * step_results receives n_rve micro_fo_step_result records, the 2-D tensor
+ * taken about each record's orientation axis. */
+mfg_status mfg_batch_micro_fo_step(mfg_batch* batch, const double* params, double* step_results);
+
 /* ---- solve without allocating ------------------------------------------ */
 /* Size of the device array that mfg_batch_run_device_noalloc() takes its
  * scratch from (16 MiB). Every GPU that loads this library holds it until the

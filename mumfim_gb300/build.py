@@ -31,6 +31,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = [
     ("mfg_host.cpp", "cxx", []),
     ("netgen.cpp", "cxx", []),
+    ("mfg_coupling.cpp", "cxx", []),
     ("mfg_relax_f64.cu", "cuda", ["--fmad=false"]),
     ("mfg_aux.cu", "cuda", ["--fmad=false"]),
     ("mfg_relax_mixed.cu", "cuda", []),

@@ -40,6 +40,15 @@ mfg_status fail(mfg_status s, const char* fmt, ...) {
   return s;
 }
 
+}  // namespace
+
+namespace mfg {
+// Error message for mfg_last_error() from the library's other host files.
+mfg_status set_error(mfg_status s, const char* msg) { return fail(s, "%s", msg); }
+}  // namespace mfg
+
+namespace {
+
 #define MFG_CUDA(call)                                                                   \
   do {                                                                                   \
     cudaError_t e_ = (call);                                                             \

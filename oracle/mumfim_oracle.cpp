@@ -352,6 +352,21 @@ void orc_nodal_mass(int32_t n_nodes, const double* coords, int32_t n_fibers,
   }
 }
 
+double orc_scale_conversion(int32_t n_nodes, const double* coords, int32_t n_fibers,
+                            const int32_t* conn, double fiber_radius, double volume_fraction) {
+  // MultiscaleCoupling.cc:7-23: the RVE edge d = sqrt(L A / vf) from the
+  // summed edge lengths L (calcDimMeasures, Utility_impl.h:6-17, summed with
+  // std::accumulate) and A = pi r^2 (MultiscaleRVEAnalysis.cc:162-163);
+  // the conversion factor is 1 / d^2.
+  std::vector<double> X(coords, coords + 3 * n_nodes);
+  double total = 0.0;
+  for (int e = 0; e < n_fibers; ++e) total += element_length(X, conn[2 * e], conn[2 * e + 1]);
+  const double pi = 4 * std::atan(1.0);
+  const double fbr_area = pi * fiber_radius * fiber_radius;
+  const double rve_dim = std::sqrt(total * fbr_area / volume_fraction);
+  return 1 / (rve_dim * rve_dim);
+}
+
 orc_batch* orc_batch_create(const mfg_network* nets, const mfg_strategy* ss, int32_t n_rve) {
   if (!nets || !ss || n_rve < 1) return nullptr;
   auto b = std::make_unique<orc_batch>();

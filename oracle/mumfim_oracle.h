@@ -44,6 +44,10 @@ void orc_reorder_permutation(int32_t n_vert, const int32_t* fixed, int32_t n_fix
                              int32_t* perm);
 /* Boundary node ids of a network in mesh order (RVE.h:86-103), returns count. */
 int32_t orc_boundary_nodes(int32_t n_nodes, const double* coords, int32_t* out);
+/* Scale conversion 1 / d^2 of the multiscale coupling
+ * (MultiscaleCoupling.cc:7-23). */
+double orc_scale_conversion(int32_t n_nodes, const double* coords, int32_t n_fibers,
+                            const int32_t* conn, double fiber_radius, double volume_fraction);
 /* Row-sum lumped nodal mass (MassIntegrator.cc:16-56), original order. */
 void orc_nodal_mass(int32_t n_nodes, const double* coords, int32_t n_fibers,
                     const int32_t* conn, double density, double area, double* mass);

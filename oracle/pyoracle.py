@@ -66,6 +66,9 @@ def lib():
                                               C.POINTER(C.c_int32)]
         L.orc_boundary_nodes.restype = C.c_int32
         L.orc_boundary_nodes.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int32)]
+        L.orc_scale_conversion.restype = C.c_double
+        L.orc_scale_conversion.argtypes = [C.c_int32, C.POINTER(C.c_double), C.c_int32,
+                                           C.POINTER(C.c_int32), C.c_double, C.c_double]
         L.orc_nodal_mass.argtypes = [C.c_int32, C.POINTER(C.c_double), C.c_int32,
                                      C.POINTER(C.c_int32), C.c_double, C.c_double,
                                      C.POINTER(C.c_double)]
@@ -156,3 +159,11 @@ def nodal_mass(coords, conn, density, area):
     lib().orc_nodal_mass(coords.shape[0], dptr(coords), conn.shape[0],
                          conn.ctypes.data_as(C.POINTER(C.c_int32)), density, area, dptr(m))
     return m
+
+
+def scale_conversion(coords, conn, fiber_radius, volume_fraction):
+    coords = np.ascontiguousarray(coords, dtype=np.float64)
+    conn = np.ascontiguousarray(conn, dtype=np.int32)
+    return lib().orc_scale_conversion(coords.shape[0], dptr(coords), conn.shape[0],
+                                      conn.ctypes.data_as(C.POINTER(C.c_int32)),
+                                      float(fiber_radius), float(volume_fraction))
