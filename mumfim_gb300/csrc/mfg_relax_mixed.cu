@@ -34,6 +34,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -53,13 +54,16 @@ struct MixedState {
   float2* mass = nullptr;  // nt, (1 / m, m)
   float4* fcon = nullptr;  // et, (X[n2] - X[n1], 1 / l0) rounded to FP32
   float4* nrm = nullptr;   // et, per-fiber force vectors (scratch; w unused)
-  // Where a cluster-solved RVE keeps what its passes read: per fiber slot the
-  // two end nodes as (owner CTA << 24 | local record), per CSR incidence the
-  // force vector as (owner CTA << 24 | local slot << 1 | end). Single-CTA
-  // RVEs use the plain node ids and incidence codes of the batch.
+  // Cluster-solved RVEs have their own fiber order (see cluster_order): per
+  // fiber position the two end nodes as (owner CTA << 24 | local record) and
+  // the read-only data, per CSR incidence the force vector as (owner CTA << 24
+  // | local position << 1 | end), or (position << 1 | end) when the force
+  // vectors are in global memory. Single-CTA RVEs use the batch's own order,
+  // node ids and incidence codes.
   int2* econn = nullptr;      // et
+  float4* fconc = nullptr;    // et
   int32_t* icode = nullptr;   // 2 * et
-  int32_t* rve_part = nullptr;  // per RVE: cluster size | (force vectors on chip) << 8
+  int32_t* mslot = nullptr;   // et, position of each fiber slot in that order
   int sms = 1;
   int smem_bytes = 0;
   // Size buckets of the batch run (kBucket[q]: cluster size, force vectors
@@ -108,36 +112,7 @@ __global__ void mixed_prepare_fibers_kernel(const DevBatch b, MixedState ms) {
       dx[k] = static_cast<float>(X[c.y] - X[c.x]);
     }
     ms.fcon[fo] = make_float4(dx[0], dx[1], dx[2], static_cast<float>(1.0 / b.l0[fo]));
-    const int part = ms.rve_part[rve];
-    const int cl = part & 0xFF;
-    if (cl > 1) {
-      // node j -> (owner, record): free and boundary nodes are split
-      // separately into cl blocks (the layout solve_rve_mixed uses)
-      const int NF = d.n_free, NB = d.n_nodes - d.n_free;
-      const int fchunk = (NF + cl - 1) / cl, bchunk = (NB + cl - 1) / cl;
-      auto code = [&](int j) {
-        int o, local;
-        if (j < NF) {
-          o = j / fchunk;
-          local = j - o * fchunk;
-        } else {
-          o = (j - NF) / bchunk;
-          local = fchunk + (j - NF) - o * bchunk;
-        }
-        return (o << 24) | local;
-      };
-      ms.econn[fo] = make_int2(code(c.x), code(c.y));
-      if (part >> 8) {
-        const int echunk = (d.n_fibers + cl - 1) / cl;
-        for (int q = 0; q < 2; ++q) {
-          const int64_t pi = d.inc_off + 2 * static_cast<int64_t>(e) + q;
-          const int ic = b.inc[pi];
-          const int slot = ic >> 1;
-          const int o = slot / echunk;
-          ms.icode[pi] = (o << 24) | ((slot - o * echunk) << 1) | (ic & 1);
-        }
-      }
-    }
+    ms.fconc[d.fiber_off + ms.mslot[fo]] = ms.fcon[fo];
   }
 }
 
@@ -500,14 +475,16 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   Forces fv;       // every fiber force vector of the RVE (node pass)
   r.e_base = 0;
   r.conn = b.conn + fo;
+  r.fcon = ms.fcon + fo;
   r.inc = b.inc + d.inc_off;
   if constexpr (CL > 1) {
     float* nodes = smem;
     r.conn = ms.econn + fo;
+    r.fcon = ms.fconc + fo;
+    r.inc = ms.icode + d.inc_off;
     if constexpr (kAll) {
       r.n = reinterpret_cast<float4*>(smem);
       r.e_base = e_lo;
-      r.inc = ms.icode + d.inc_off;
       fv.base = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
       nodes = smem + 4 * echunk;
     } else {
@@ -541,7 +518,6 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
     u = own;
   }
   r.mass = ms.mass + no;
-  r.fcon = ms.fcon + fo;
   r.rowptr = b.rowptr + d.row_off;
   r.ramp = reinterpret_cast<float*>(b.ramp + 6 * d.bnd_off);  // 12 floats per boundary node
   const double* F = a.F + 9 * (a.n_F > 1 ? rve : 0);
@@ -804,7 +780,8 @@ MixedState* mixed_new() { return new MixedState(); }
 void mixed_destroy(MixedState* ms) {
   if (!ms) return;
   for (void* p : {static_cast<void*>(ms->u_hl), static_cast<void*>(ms->econn),
-                  static_cast<void*>(ms->icode), static_cast<void*>(ms->rve_part),
+                  static_cast<void*>(ms->icode), static_cast<void*>(ms->mslot),
+                  static_cast<void*>(ms->fconc),
                   static_cast<void*>(ms->v), static_cast<void*>(ms->mass),
                   static_cast<void*>(ms->fcon), static_cast<void*>(ms->nrm),
                   static_cast<void*>(ms->order), static_cast<void*>(ms->queues)})
@@ -833,6 +810,64 @@ int bucket_of(const RveDesc& d, int smem_floats) {
         smem_floats)
       return q;
   return kBuckets - 1;
+}
+
+// Fiber order of an RVE solved by a cluster of cl CTAs. Each fiber goes to
+// the CTA that owns its lower-numbered end (a free node whenever the fiber
+// has one); within a CTA, fibers with both ends owned by that CTA come
+// first, then the fibers that cross to another CTA, each group in slot
+// order. CTA o then computes positions [o*echunk, (o+1)*echunk): most warps
+// see only local end nodes, a load of about 37 cycles through the cluster
+// window against about 200 for a peer CTA's shared memory. Writes the
+// positions (mslot), the end-node codes by position (econn) and the
+// force-vector codes of the CSR incidences (icode). Single-CTA RVEs keep
+// the batch's order, so their entries mirror conn and inc.
+void cluster_order(const RveDesc& d, int cl, bool all, const std::vector<int2>& conn,
+                   const std::vector<int32_t>& inc, std::vector<int2>& econn,
+                   std::vector<int32_t>& icode, std::vector<int32_t>& mslot) {
+  const int E = d.n_fibers, NF = d.n_free, NB = d.n_nodes - d.n_free;
+  const int64_t fo = d.fiber_off, io = d.inc_off;
+  if (cl == 1) {
+    for (int e = 0; e < E; ++e) {
+      mslot[fo + e] = e;
+      econn[fo + e] = conn[fo + e];
+    }
+    for (int64_t p = 0; p < 2LL * E; ++p) icode[io + p] = inc[io + p];
+    return;
+  }
+  const int fchunk = (NF + cl - 1) / cl, bchunk = (NB + cl - 1) / cl;
+  auto owner = [&](int j) { return j < NF ? j / fchunk : (j - NF) / bchunk; };
+  auto code = [&](int j) {
+    const int o = owner(j);
+    const int local = j < NF ? j - o * fchunk : fchunk + (j - NF) - o * bchunk;
+    return (o << 24) | local;
+  };
+  // stable counting sort by (owner of the lower end, crossing)
+  std::vector<int> key(E), start(2 * cl + 1, 0);
+  for (int e = 0; e < E; ++e) {
+    const int2 c = conn[fo + e];
+    const int o = owner(std::min(c.x, c.y));
+    key[e] = 2 * o + ((owner(c.x) == o && owner(c.y) == o) ? 0 : 1);
+    ++start[key[e] + 1];
+  }
+  for (int k = 0; k < 2 * cl; ++k) start[k + 1] += start[k];
+  for (int e = 0; e < E; ++e) {
+    const int m = start[key[e]]++;
+    mslot[fo + e] = m;
+    const int2 c = conn[fo + e];
+    econn[fo + m] = make_int2(code(c.x), code(c.y));
+  }
+  const int echunk = (E + cl - 1) / cl;
+  for (int64_t p = 0; p < 2LL * E; ++p) {
+    const int ic = inc[io + p];
+    const int m = mslot[fo + (ic >> 1)];
+    if (all) {
+      const int o = m / echunk;
+      icode[io + p] = (o << 24) | ((m - o * echunk) << 1) | (ic & 1);
+    } else {
+      icode[io + p] = (m << 1) | (ic & 1);
+    }
+  }
 }
 
 template <int CL, bool kAll>
@@ -889,7 +924,8 @@ cudaError_t setup_bucket(MixedState& ms, int n, int q) {
 }  // namespace
 
 cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<RveDesc>& desc,
-                         int sms, cudaStream_t s) {
+                         const std::vector<int2>& conn, const std::vector<int32_t>& inc, int sms,
+                         cudaStream_t s) {
   cudaError_t e;
   const size_t nt = static_cast<size_t>(b.nt), et = static_cast<size_t>(b.et);
   if ((e = alloc(&ms.u_hl, 6 * nt)) != cudaSuccess) return e;
@@ -898,8 +934,9 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
   if ((e = alloc(&ms.fcon, et)) != cudaSuccess) return e;
   if ((e = alloc(&ms.nrm, et)) != cudaSuccess) return e;
   if ((e = alloc(&ms.econn, et)) != cudaSuccess) return e;
+  if ((e = alloc(&ms.fconc, et)) != cudaSuccess) return e;
   if ((e = alloc(&ms.icode, 2 * et)) != cudaSuccess) return e;
-  if ((e = alloc(&ms.rve_part, desc.size())) != cudaSuccess) return e;
+  if ((e = alloc(&ms.mslot, et)) != cudaSuccess) return e;
   if ((e = alloc(&ms.order, desc.size())) != cudaSuccess) return e;
   if ((e = alloc(&ms.queues, kBuckets)) != cudaSuccess) return e;
   ms.sms = sms;
@@ -911,16 +948,32 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
 
   // size buckets, each in longest-processing-time order
   std::vector<std::vector<int32_t>> bucket(kBuckets);
-  std::vector<int32_t> part(desc.size());
+  std::vector<int> rve_q(desc.size());
   for (size_t r = 0; r < desc.size(); ++r) {
-    const int q = bucket_of(desc[r], smem_floats);
-    bucket[q].push_back(static_cast<int32_t>(r));
-    part[r] = kBucket[q].cl | (kBucket[q].all ? 1 << 8 : 0);
+    rve_q[r] = bucket_of(desc[r], smem_floats);
+    bucket[rve_q[r]].push_back(static_cast<int32_t>(r));
   }
-  if (!part.empty() &&
-      (e = cudaMemcpy(ms.rve_part, part.data(), part.size() * sizeof(int32_t),
-                      cudaMemcpyHostToDevice)) != cudaSuccess)
-    return e;
+  {
+    // fiber order and codes of the cluster-solved RVEs
+    std::vector<int2> econn(et);
+    std::vector<int32_t> icode(2 * et), mslot(et);
+    std::vector<std::thread> pool;
+    const int nthr = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    for (int t = 0; t < nthr; ++t)
+      pool.emplace_back([&, t] {
+        for (size_t r = t; r < desc.size(); r += nthr)
+          cluster_order(desc[r], kBucket[rve_q[r]].cl, kBucket[rve_q[r]].all, conn, inc, econn,
+                        icode, mslot);
+      });
+    for (auto& th : pool) th.join();
+    if ((e = cudaMemcpy(ms.econn, econn.data(), et * sizeof(int2), cudaMemcpyHostToDevice)) !=
+            cudaSuccess ||
+        (e = cudaMemcpy(ms.icode, icode.data(), 2 * et * sizeof(int32_t),
+                        cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(ms.mslot, mslot.data(), et * sizeof(int32_t), cudaMemcpyHostToDevice)) !=
+            cudaSuccess)
+      return e;
+  }
   std::vector<int32_t> order;
   order.reserve(desc.size());
   for (int q = 0; q < kBuckets; ++q) {
