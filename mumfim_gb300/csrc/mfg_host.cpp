@@ -590,7 +590,7 @@ mfg_status mfg_batch_create(const mfg_network* nets, const mfg_strategy* strateg
   dv.queue = b->d_queue.p;
   if (b->precision == MFG_PREC_MIXED) {
     b->mixed.reset(mfg::mixed_new());
-    cudaError_t e = b->mixed ? mfg::mixed_create(*b->mixed, dv, b->desc, conn, inc, b->sms, s)
+    cudaError_t e = b->mixed ? mfg::mixed_create(*b->mixed, dv, b->desc, conn, rowptr, inc, b->sms, s)
                              : cudaErrorMemoryAllocation;
     if (e != cudaSuccess)
       return fail(e == cudaErrorMemoryAllocation ? MFG_E_OOM : MFG_E_CUDA,
@@ -887,7 +887,7 @@ struct PendingReq {
 // working set when used), for admission against the HBM budget.
 double batch_bytes(int64_t nt, int64_t et, int64_t nbt, int64_t R, bool mixed) {
   double b = nt * (5 * 3 * 8.0 + 8 + 4) + et * (8.0 + 8 + 24 + 8) + nbt * (48.0 + 4) + R * 200.0;
-  if (mixed) b += nt * (24.0 + 12 + 8) + et * (16.0 + 16 + 16 + 8 + 8 + 4) + R * 8.0;
+  if (mixed) b += nt * (24.0 + 12 + 8 + 4 + 4 + 8) + et * (16.0 + 16 + 16 + 8 + 8 + 4) + R * 12.0;
   return b;
 }
 

@@ -64,6 +64,12 @@ struct MixedState {
   float4* fconc = nullptr;    // et
   int32_t* icode = nullptr;   // 2 * et
   int32_t* mslot = nullptr;   // et, position of each fiber slot in that order
+  // Their nodes: each CTA's free nodes whose force vectors are all its own
+  // come first (all-on-chip buckets); gnode maps a node position to the
+  // batch node index, and the CSR rows and masses follow the positions.
+  int32_t* gnode = nullptr;    // nt
+  int32_t* mrowptr = nullptr;  // nt + n_rve
+  float2* mmass = nullptr;     // nt
   int sms = 1;
   int smem_bytes = 0;
   // Size buckets of the batch run (kBucket[q]: cluster size, force vectors
@@ -97,6 +103,11 @@ __global__ void mixed_prepare_kernel(const DevBatch b, MixedState ms) {
     const double m = b.m[i];
     ms.mass[i] = make_float2(static_cast<float>(1.0 / m), static_cast<float>(m));
   }
+}
+
+__global__ void mixed_prepare_order_kernel(const DevBatch b, MixedState ms) {
+  const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (i < b.nt) ms.mmass[i] = ms.mass[ms.gnode[i]];
 }
 
 __global__ void mixed_prepare_fibers_kernel(const DevBatch b, MixedState ms) {
@@ -477,11 +488,15 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   r.conn = b.conn + fo;
   r.fcon = ms.fcon + fo;
   r.inc = b.inc + d.inc_off;
+  r.rowptr = b.rowptr + d.row_off;
+  r.mass = ms.mass + no;
   if constexpr (CL > 1) {
     float* nodes = smem;
     r.conn = ms.econn + fo;
     r.fcon = ms.fconc + fo;
     r.inc = ms.icode + d.inc_off;
+    r.rowptr = ms.mrowptr + d.row_off;
+    r.mass = ms.mmass + no;
     if constexpr (kAll) {
       r.n = reinterpret_cast<float4*>(smem);
       r.e_base = e_lo;
@@ -517,8 +532,6 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
     fv.p = r.n;
     u = own;
   }
-  r.mass = ms.mass + no;
-  r.rowptr = b.rowptr + d.row_off;
   r.ramp = reinterpret_cast<float*>(b.ramp + 6 * d.bnd_off);  // 12 floats per boundary node
   const double* F = a.F + 9 * (a.n_F > 1 ? rve : 0);
   const bool ramp = d.mode == 1;
@@ -531,12 +544,13 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   for (int t = tid; t < n_own; t += kThreadsMixed) {
     const int i = t < nfo ? f_lo + t : g_lo + (t - nfo);
     const int li = t < nfo ? t : fchunk + (t - nfo);
+    const int64_t gi = CL > 1 ? __ldg(ms.gnode + no + i) : no + i;  // batch node index
     double xo[3], up[3], X[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      xo[k] = b.x[k * nt + no + i];
-      up[k] = b.u[k * nt + no + i];
-      X[k] = b.X[k * nt + no + i];
+      xo[k] = b.x[k * nt + gi];
+      up[k] = b.u[k * nt + gi];
+      X[k] = b.X[k * nt + gi];
     }
     if (!ramp) {
       const double u0 = (Fm[0] - 1) * xo[0] + Fm[1] * xo[1] + Fm[2] * xo[2] + up[0];
@@ -672,13 +686,14 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   for (int t = tid; t < n_own; t += kThreadsMixed) {
     const int i = t < nfo ? f_lo + t : g_lo + (t - nfo);
     const int li = t < nfo ? t : fchunk + (t - nfo);
+    const int64_t gi = CL > 1 ? __ldg(ms.gnode + no + i) : no + i;  // batch node index
     const NodeRec nr = load_rec(own.rec(li));
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const double Xk = b.X[k * nt + no + i];
+      const double Xk = b.X[k * nt + gi];
       const double xk = Xk + (static_cast<double>(nr.hi[k]) + nr.lo[k]);
-      b.x[k * nt + no + i] = xk;
-      if (a.update_coords) b.u[k * nt + no + i] = xk - Xk;
+      b.x[k * nt + gi] = xk;
+      if (a.update_coords) b.u[k * nt + gi] = xk - Xk;
     }
     if (i >= NF) {
       float a0, a1, a2;
@@ -781,6 +796,8 @@ void mixed_destroy(MixedState* ms) {
   if (!ms) return;
   for (void* p : {static_cast<void*>(ms->u_hl), static_cast<void*>(ms->econn),
                   static_cast<void*>(ms->icode), static_cast<void*>(ms->mslot),
+                  static_cast<void*>(ms->gnode), static_cast<void*>(ms->mrowptr),
+                  static_cast<void*>(ms->mmass),
                   static_cast<void*>(ms->fconc),
                   static_cast<void*>(ms->v), static_cast<void*>(ms->mass),
                   static_cast<void*>(ms->fcon), static_cast<void*>(ms->nrm),
@@ -812,37 +829,44 @@ int bucket_of(const RveDesc& d, int smem_floats) {
   return kBuckets - 1;
 }
 
-// Fiber order of an RVE solved by a cluster of cl CTAs. Each fiber goes to
-// the CTA that owns its lower-numbered end (a free node whenever the fiber
-// has one); within a CTA, fibers with both ends owned by that CTA come
-// first, then the fibers that cross to another CTA, each group in slot
-// order. CTA o then computes positions [o*echunk, (o+1)*echunk): most warps
-// see only local end nodes, a load of about 37 cycles through the cluster
-// window against about 200 for a peer CTA's shared memory. Writes the
-// positions (mslot), the end-node codes by position (econn) and the
-// force-vector codes of the CSR incidences (icode). Single-CTA RVEs keep
-// the batch's order, so their entries mirror conn and inc.
+// Fiber and node order of an RVE solved by a cluster of cl CTAs.
+//
+// Fibers: each goes to the CTA that owns its lower-numbered end (a free node
+// whenever the fiber has one); within a CTA, fibers with both ends owned by
+// that CTA come first, then the fibers that cross to another CTA, each group
+// in slot order. CTA o computes positions [o*echunk, (o+1)*echunk), so most
+// warps see only local end nodes: a load of about 37 cycles through the
+// cluster window against about 200 for a peer CTA's shared memory.
+//
+// Nodes (buckets with the force vectors on chip): within each CTA's block of
+// free nodes, those whose incident force vectors are all computed by the
+// same CTA come first, so the gathers of most warps stay local too. Boundary
+// nodes keep their places.
+//
+// Writes the fiber positions (mslot), the end-node codes by position
+// (econn), the node index by node position (gnode, batch-wide), the CSR rows
+// by node position (mrowptr) and the force-vector codes of their incidences
+// (icode). Single-CTA RVEs keep the batch's order.
 void cluster_order(const RveDesc& d, int cl, bool all, const std::vector<int2>& conn,
-                   const std::vector<int32_t>& inc, std::vector<int2>& econn,
-                   std::vector<int32_t>& icode, std::vector<int32_t>& mslot) {
-  const int E = d.n_fibers, NF = d.n_free, NB = d.n_nodes - d.n_free;
-  const int64_t fo = d.fiber_off, io = d.inc_off;
+                   const std::vector<int32_t>& rowptr, const std::vector<int32_t>& inc,
+                   std::vector<int2>& econn, std::vector<int32_t>& icode,
+                   std::vector<int32_t>& mslot, std::vector<int32_t>& gnode,
+                   std::vector<int32_t>& mrowptr) {
+  const int N = d.n_nodes, E = d.n_fibers, NF = d.n_free, NB = d.n_nodes - d.n_free;
+  const int64_t fo = d.fiber_off, io = d.inc_off, no = d.node_off, ro = d.row_off;
   if (cl == 1) {
     for (int e = 0; e < E; ++e) {
       mslot[fo + e] = e;
       econn[fo + e] = conn[fo + e];
     }
     for (int64_t p = 0; p < 2LL * E; ++p) icode[io + p] = inc[io + p];
+    for (int j = 0; j < N; ++j) gnode[no + j] = static_cast<int32_t>(no + j);
+    for (int j = 0; j <= N; ++j) mrowptr[ro + j] = rowptr[ro + j];
     return;
   }
   const int fchunk = (NF + cl - 1) / cl, bchunk = (NB + cl - 1) / cl;
   auto owner = [&](int j) { return j < NF ? j / fchunk : (j - NF) / bchunk; };
-  auto code = [&](int j) {
-    const int o = owner(j);
-    const int local = j < NF ? j - o * fchunk : fchunk + (j - NF) - o * bchunk;
-    return (o << 24) | local;
-  };
-  // stable counting sort by (owner of the lower end, crossing)
+  // fibers: stable counting sort by (owner of the lower end, crossing)
   std::vector<int> key(E), start(2 * cl + 1, 0);
   for (int e = 0; e < E; ++e) {
     const int2 c = conn[fo + e];
@@ -851,22 +875,54 @@ void cluster_order(const RveDesc& d, int cl, bool all, const std::vector<int2>& 
     ++start[key[e] + 1];
   }
   for (int k = 0; k < 2 * cl; ++k) start[k + 1] += start[k];
-  for (int e = 0; e < E; ++e) {
-    const int m = start[key[e]]++;
-    mslot[fo + e] = m;
-    const int2 c = conn[fo + e];
-    econn[fo + m] = make_int2(code(c.x), code(c.y));
-  }
+  for (int e = 0; e < E; ++e) mslot[fo + e] = start[key[e]]++;
   const int echunk = (E + cl - 1) / cl;
-  for (int64_t p = 0; p < 2LL * E; ++p) {
-    const int ic = inc[io + p];
-    const int m = mslot[fo + (ic >> 1)];
-    if (all) {
-      const int o = m / echunk;
-      icode[io + p] = (o << 24) | ((m - o * echunk) << 1) | (ic & 1);
-    } else {
-      icode[io + p] = (m << 1) | (ic & 1);
+  // nodes: position of each node (identity but for the free blocks of the
+  // on-chip buckets, where local-only nodes go first)
+  std::vector<int> pos(N);
+  for (int j = 0; j < N; ++j) pos[j] = j;
+  if (all) {
+    for (int o = 0; o < cl; ++o) {
+      const int f_lo = std::min(NF, o * fchunk), f_hi = std::min(NF, f_lo + fchunk);
+      std::vector<int> local, cut;
+      for (int j = f_lo; j < f_hi; ++j) {
+        bool own = true;
+        for (int p = rowptr[ro + j]; p < rowptr[ro + j + 1] && own; ++p)
+          own = mslot[fo + (inc[io + p] >> 1)] / echunk == o;
+        (own ? local : cut).push_back(j);
+      }
+      int q = f_lo;
+      for (int j : local) pos[j] = q++;
+      for (int j : cut) pos[j] = q++;
     }
+  }
+  auto code = [&](int j) {
+    const int o = owner(j);
+    const int local = j < NF ? pos[j] - o * fchunk : fchunk + (j - NF) - o * bchunk;
+    return (o << 24) | local;
+  };
+  for (int e = 0; e < E; ++e) {
+    const int2 c = conn[fo + e];
+    econn[fo + mslot[fo + e]] = make_int2(code(c.x), code(c.y));
+  }
+  std::vector<int> at(N);
+  for (int j = 0; j < N; ++j) at[pos[j]] = j;
+  int64_t q = 0;
+  mrowptr[ro] = 0;
+  for (int P = 0; P < N; ++P) {
+    const int j = at[P];
+    gnode[no + P] = static_cast<int32_t>(no + j);
+    for (int p = rowptr[ro + j]; p < rowptr[ro + j + 1]; ++p, ++q) {
+      const int ic = inc[io + p];
+      const int m = mslot[fo + (ic >> 1)];
+      if (all) {
+        const int o = m / echunk;
+        icode[io + q] = (o << 24) | ((m - o * echunk) << 1) | (ic & 1);
+      } else {
+        icode[io + q] = (m << 1) | (ic & 1);
+      }
+    }
+    mrowptr[ro + P + 1] = static_cast<int32_t>(q);
   }
 }
 
@@ -924,8 +980,8 @@ cudaError_t setup_bucket(MixedState& ms, int n, int q) {
 }  // namespace
 
 cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<RveDesc>& desc,
-                         const std::vector<int2>& conn, const std::vector<int32_t>& inc, int sms,
-                         cudaStream_t s) {
+                         const std::vector<int2>& conn, const std::vector<int32_t>& rowptr,
+                         const std::vector<int32_t>& inc, int sms, cudaStream_t s) {
   cudaError_t e;
   const size_t nt = static_cast<size_t>(b.nt), et = static_cast<size_t>(b.et);
   if ((e = alloc(&ms.u_hl, 6 * nt)) != cudaSuccess) return e;
@@ -937,6 +993,9 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
   if ((e = alloc(&ms.fconc, et)) != cudaSuccess) return e;
   if ((e = alloc(&ms.icode, 2 * et)) != cudaSuccess) return e;
   if ((e = alloc(&ms.mslot, et)) != cudaSuccess) return e;
+  if ((e = alloc(&ms.gnode, nt)) != cudaSuccess) return e;
+  if ((e = alloc(&ms.mrowptr, rowptr.size())) != cudaSuccess) return e;
+  if ((e = alloc(&ms.mmass, nt)) != cudaSuccess) return e;
   if ((e = alloc(&ms.order, desc.size())) != cudaSuccess) return e;
   if ((e = alloc(&ms.queues, kBuckets)) != cudaSuccess) return e;
   ms.sms = sms;
@@ -956,14 +1015,14 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
   {
     // fiber order and codes of the cluster-solved RVEs
     std::vector<int2> econn(et);
-    std::vector<int32_t> icode(2 * et), mslot(et);
+    std::vector<int32_t> icode(2 * et), mslot(et), gnode(nt), mrowptr(rowptr.size());
     std::vector<std::thread> pool;
     const int nthr = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
     for (int t = 0; t < nthr; ++t)
       pool.emplace_back([&, t] {
         for (size_t r = t; r < desc.size(); r += nthr)
-          cluster_order(desc[r], kBucket[rve_q[r]].cl, kBucket[rve_q[r]].all, conn, inc, econn,
-                        icode, mslot);
+          cluster_order(desc[r], kBucket[rve_q[r]].cl, kBucket[rve_q[r]].all, conn, rowptr, inc,
+                        econn, icode, mslot, gnode, mrowptr);
       });
     for (auto& th : pool) th.join();
     if ((e = cudaMemcpy(ms.econn, econn.data(), et * sizeof(int2), cudaMemcpyHostToDevice)) !=
@@ -971,7 +1030,11 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
         (e = cudaMemcpy(ms.icode, icode.data(), 2 * et * sizeof(int32_t),
                         cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(ms.mslot, mslot.data(), et * sizeof(int32_t), cudaMemcpyHostToDevice)) !=
-            cudaSuccess)
+            cudaSuccess ||
+        (e = cudaMemcpy(ms.gnode, gnode.data(), nt * sizeof(int32_t), cudaMemcpyHostToDevice)) !=
+            cudaSuccess ||
+        (e = cudaMemcpy(ms.mrowptr, mrowptr.data(), mrowptr.size() * sizeof(int32_t),
+                        cudaMemcpyHostToDevice)) != cudaSuccess)
       return e;
   }
   std::vector<int32_t> order;
@@ -1007,6 +1070,8 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
 
   const int64_t n = std::max<int64_t>(b.nt, 1);
   mixed_prepare_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(b, ms);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  mixed_prepare_order_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(b, ms);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   int max_e = 1;
   for (const RveDesc& d : desc) max_e = std::max(max_e, d.n_fibers);
