@@ -203,8 +203,11 @@ __device__ __forceinline__ void split(double u, float& hi, float& lo) {
 struct Rve {
   RveDesc d;
   Law L;
-  float4* n;            // this CTA's fiber force vectors, indexed by slot - e_base
-  int e_base;
+  // This CTA's fiber force vectors: position e is kept in shared memory at
+  // n[e - e_base] when e - e_base < nk, else in global memory at ng[e].
+  float4* n;
+  int e_base, nk;
+  float4* ng;
   const float2* mass;   // (1 / m, m)
   const float4* fcon;   // (dX, 1 / l0)
   const int2* conn;     // end nodes (node ids, or cluster codes)
@@ -287,6 +290,28 @@ struct ClusterForces {
                  : "=f"(t.x), "=f"(t.y), "=f"(t.z), "=f"(t.w)
                  : "r"(a));
     return t;
+  }
+};
+
+// Force vectors of an RVE whose clusters keep part of them in shared memory:
+// an incidence code with kSmemFlag set reads CTA o's shared memory at its
+// local position, any other reads global memory at its position.
+constexpr int kSmemFlag = 1 << 30;
+template <int CL>
+struct HybridForces {
+  uint32_t base;
+  const float4* g;
+  __device__ __forceinline__ float4 load(int code) const {
+    if (code & kSmemFlag) {
+      const uint32_t o = (static_cast<uint32_t>(code) >> 24) & 7u;
+      const uint32_t a = cluster_addr(base + 8u * (static_cast<uint32_t>(code) & 0xFFFFFEu), o);
+      float4 t;
+      asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+                   : "=f"(t.x), "=f"(t.y), "=f"(t.z), "=f"(t.w)
+                   : "r"(a));
+      return t;
+    }
+    return g[code >> 1];
   }
 };
 
@@ -389,7 +414,7 @@ __device__ __forceinline__ NodeConst load_node(const Rve& r, int i) {
 // would cancel.
 // Returns the current length l0 sqrt(1 + 2g), which the critical time step
 // needs every 100 steps (unused, and so not computed, on the other steps).
-template <class Nodes>
+template <bool kSplit, class Nodes>
 __device__ __forceinline__ float fiber_force(const Rve& r, const Nodes& u, int e,
                                              const FiberConst& k) {
   const NodeRec na = u.load(k.c.x), nb = u.load(k.c.y);
@@ -405,15 +430,20 @@ __device__ __forceinline__ float fiber_force(const Rve& r, const Nodes& u, int e
                         fmaf(du[1], fmaf(0.5f, du[1], fc.y), du[2] * fmaf(0.5f, du[2], fc.z)));
   const float g = gn * (fc.w * fc.w);
   const float t = tension_over_length(r.L, g, fc.w);
-  r.n[e - r.e_base] =
-      make_float4((fc.x + du[0]) * t, (fc.y + du[1]) * t, (fc.z + du[2]) * t, 0.f);
+  const float4 f = make_float4((fc.x + du[0]) * t, (fc.y + du[1]) * t, (fc.z + du[2]) * t, 0.f);
+  const int le = e - r.e_base;
+  if (!kSplit || le < r.nk)
+    r.n[le] = f;
+  else
+    r.ng[e] = f;
   return sqrtf(fmaxf(fmaf(2.f, g, 1.f), 0.f)) / fc.w;
 }
 
 // Force vectors of fiber slots e_lo + tid, + kThreadsMixed, ... < e_hi, the
 // next slot's read-only data loaded while the current one is computed.
-// Returns the shortest current length among them when kLen.
-template <bool kLen, class Nodes>
+// Returns the shortest current length among them when kLen. kSplit: the
+// force vectors may be partly in global memory (r.nk < the CTA's count).
+template <bool kLen, bool kSplit, class Nodes>
 __device__ __forceinline__ float fiber_pass(const Rve& r, const Nodes& u, int e_lo, int e_hi) {
   float lmin = FLT_MAX;
   int e = e_lo + static_cast<int>(threadIdx.x);
@@ -424,7 +454,7 @@ __device__ __forceinline__ float fiber_pass(const Rve& r, const Nodes& u, int e_
     const bool more = en < e_hi;
     FiberConst nxt = cur;
     if (more) nxt = load_fiber(r, en);
-    const float l = fiber_force(r, u, e, cur);
+    const float l = fiber_force<kSplit>(r, u, e, cur);
     if (kLen) lmin = fminf(lmin, l);
     if (!more) break;
     cur = nxt;
@@ -443,6 +473,14 @@ __host__ __device__ inline int64_t cluster_floats(int n_nodes, int n_free, int n
   const int64_t cap = (static_cast<int64_t>(n_free) + cl - 1) / cl + (nb + cl - 1) / cl;
   const int64_t echunk = (static_cast<int64_t>(n_fibers) + cl - 1) / cl;
   return 9 * cap + (all ? 4 * echunk : 0);
+}
+
+// Force-vector slots a CTA of a node-state-only cluster keeps in shared
+// memory beside its 9 * cap floats of node state.
+__host__ __device__ inline int hybrid_slots(int cap, int echunk, int smem_floats) {
+  const int free_floats = smem_floats - 9 * cap;
+  if (free_floats <= 0) return 0;
+  return free_floats / 4 < echunk ? free_floats / 4 : echunk;
 }
 
 // One RVE solved by one CTA (CL = 1) or by the CL CTAs of a cluster. A CTA
@@ -479,12 +517,15 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   const int e_lo = min(E, rank * echunk);
   const int e_hi = min(E, e_lo + echunk);
   using Nodes = std::conditional_t<(CL > 1), ClusterNodes<CL>, LocalNodes>;
-  using Forces = std::conditional_t<(CL > 1 && kAll), ClusterForces<CL>, LocalForces>;
+  using Forces = std::conditional_t<
+      (CL > 1), std::conditional_t<kAll, ClusterForces<CL>, HybridForces<CL>>, LocalForces>;
   Nodes u;         // every node of the RVE (fiber pass)
   LocalNodes own;  // the node records this CTA updates, by local index
   float* vel;      // their velocities (x, y, z), by local index
   Forces fv;       // every fiber force vector of the RVE (node pass)
   r.e_base = 0;
+  r.nk = 0;
+  r.ng = ms.nrm + fo;
   r.conn = b.conn + fo;
   r.fcon = ms.fcon + fo;
   r.inc = b.inc + d.inc_off;
@@ -497,15 +538,14 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
     r.inc = ms.icode + d.inc_off;
     r.rowptr = ms.mrowptr + d.row_off;
     r.mass = ms.mmass + no;
-    if constexpr (kAll) {
-      r.n = reinterpret_cast<float4*>(smem);
-      r.e_base = e_lo;
-      fv.base = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
-      nodes = smem + 4 * echunk;
-    } else {
-      r.n = ms.nrm + fo;
-      fv.p = r.n;
-    }
+    // force vectors first: all of the CTA's, or as many as fit beside the
+    // node state (the rest in global memory)
+    r.n = reinterpret_cast<float4*>(smem);
+    r.e_base = e_lo;
+    r.nk = kAll ? echunk : hybrid_slots(cap, echunk, smem_floats);
+    fv.base = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+    if constexpr (!kAll) fv.g = r.ng;
+    nodes = smem + 4 * r.nk;
     u.base = static_cast<uint32_t>(__cvta_generic_to_shared(nodes));
     own.hl = nodes;
     vel = nodes + 6 * cap;
@@ -514,22 +554,26 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
     // velocities
     if (kAll || cluster_floats(N, NF, E, 1, true) <= smem_floats) {
       r.n = reinterpret_cast<float4*>(smem);
+      r.nk = E;
+      fv.p = r.n;
       own.hl = smem + 4 * E;
       vel = smem + 4 * E + 6 * N;
     } else if (cluster_floats(N, NF, E, 1, false) <= smem_floats) {
       r.n = ms.nrm + fo;
+      fv.p = r.ng;
       own.hl = smem;
       vel = smem + 6 * N;
     } else if (6LL * N <= smem_floats) {
       r.n = ms.nrm + fo;
+      fv.p = r.ng;
       own.hl = smem;
       vel = ms.v + 3 * no;
     } else {
       r.n = ms.nrm + fo;
+      fv.p = r.ng;
       own.hl = ms.u_hl + 6 * no;
       vel = ms.v + 3 * no;
     }
-    fv.p = r.n;
     u = own;
   }
   r.ramp = reinterpret_cast<float*>(b.ramp + 6 * d.bnd_off);  // 12 floats per boundary node
@@ -588,7 +632,7 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   Ops::sync();
   // critical step from the shortest current fiber (FP32 length from the
   // Green strain, ~1e-7 relative; h itself is an FP32 number)
-  const float lmin = fiber_pass<true>(r, u, e_lo, e_hi);
+  const float lmin = fiber_pass<true, !kAll>(r, u, e_lo, e_hi);
   double dt_crit =
       Ops::template combine<true>(block_min<kThreadsMixed>(lmin, red), cred) / d.sound_speed;
 
@@ -669,12 +713,12 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
     Ops::sync();
     const bool dt_step = (step % kUpdateFreq) == 0;
     if (dt_step) {
-      const float lm = fiber_pass<true>(r, u, e_lo, e_hi);
+      const float lm = fiber_pass<true, !kAll>(r, u, e_lo, e_hi);
       dt_crit =
           Ops::template combine<true>(block_min<kThreadsMixed>(lm, red), cred) / d.sound_speed;
       h_cur = static_cast<float>(d.crit * dt_crit * 0.5);
     } else {
-      fiber_pass<false>(r, u, e_lo, e_hi);
+      fiber_pass<false, !kAll>(r, u, e_lo, e_hi);
       Ops::sync();
     }
     h_prev = h;
@@ -838,16 +882,20 @@ int bucket_of(const RveDesc& d, int smem_floats) {
 // warps see only local end nodes: a load of about 37 cycles through the
 // cluster window against about 200 for a peer CTA's shared memory.
 //
-// Nodes (buckets with the force vectors on chip): within each CTA's block of
-// free nodes, those whose incident force vectors are all computed by the
-// same CTA come first, so the gathers of most warps stay local too. Boundary
-// nodes keep their places.
+// Force vectors: in the node-state-only buckets a CTA keeps its first K
+// positions (K = hybrid_slots) in shared memory and the rest in global
+// memory; in the others all of them in shared memory.
+//
+// Nodes: within each CTA's block of free nodes, those whose incident force
+// vectors are all in that CTA's shared memory come first, so the gathers of
+// most warps stay local too. Boundary nodes keep their places.
 //
 // Writes the fiber positions (mslot), the end-node codes by position
 // (econn), the node index by node position (gnode, batch-wide), the CSR rows
 // by node position (mrowptr) and the force-vector codes of their incidences
 // (icode). Single-CTA RVEs keep the batch's order.
-void cluster_order(const RveDesc& d, int cl, bool all, const std::vector<int2>& conn,
+void cluster_order(const RveDesc& d, int cl, bool all, int smem_floats,
+                   const std::vector<int2>& conn,
                    const std::vector<int32_t>& rowptr, const std::vector<int32_t>& inc,
                    std::vector<int2>& econn, std::vector<int32_t>& icode,
                    std::vector<int32_t>& mslot, std::vector<int32_t>& gnode,
@@ -877,18 +925,20 @@ void cluster_order(const RveDesc& d, int cl, bool all, const std::vector<int2>& 
   for (int k = 0; k < 2 * cl; ++k) start[k + 1] += start[k];
   for (int e = 0; e < E; ++e) mslot[fo + e] = start[key[e]]++;
   const int echunk = (E + cl - 1) / cl;
-  // nodes: position of each node (identity but for the free blocks of the
-  // on-chip buckets, where local-only nodes go first)
+  const int K = all ? echunk : hybrid_slots(fchunk + bchunk, echunk, smem_floats);
+  auto on_chip = [&](int m, int o) { return m / echunk == o && m - o * echunk < K; };
+  // nodes: position of each node (identity but for the free blocks, where
+  // nodes with only on-chip local force vectors go first)
   std::vector<int> pos(N);
   for (int j = 0; j < N; ++j) pos[j] = j;
-  if (all) {
+  {
     for (int o = 0; o < cl; ++o) {
       const int f_lo = std::min(NF, o * fchunk), f_hi = std::min(NF, f_lo + fchunk);
       std::vector<int> local, cut;
       for (int j = f_lo; j < f_hi; ++j) {
         bool own = true;
         for (int p = rowptr[ro + j]; p < rowptr[ro + j + 1] && own; ++p)
-          own = mslot[fo + (inc[io + p] >> 1)] / echunk == o;
+          own = on_chip(mslot[fo + (inc[io + p] >> 1)], o);
         (own ? local : cut).push_back(j);
       }
       int q = f_lo;
@@ -915,9 +965,11 @@ void cluster_order(const RveDesc& d, int cl, bool all, const std::vector<int2>& 
     for (int p = rowptr[ro + j]; p < rowptr[ro + j + 1]; ++p, ++q) {
       const int ic = inc[io + p];
       const int m = mslot[fo + (ic >> 1)];
+      const int o = m / echunk;
       if (all) {
-        const int o = m / echunk;
         icode[io + q] = (o << 24) | ((m - o * echunk) << 1) | (ic & 1);
+      } else if (m - o * echunk < K) {
+        icode[io + q] = kSmemFlag | (o << 24) | ((m - o * echunk) << 1) | (ic & 1);
       } else {
         icode[io + q] = (m << 1) | (ic & 1);
       }
@@ -1021,8 +1073,8 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
     for (int t = 0; t < nthr; ++t)
       pool.emplace_back([&, t] {
         for (size_t r = t; r < desc.size(); r += nthr)
-          cluster_order(desc[r], kBucket[rve_q[r]].cl, kBucket[rve_q[r]].all, conn, rowptr, inc,
-                        econn, icode, mslot, gnode, mrowptr);
+          cluster_order(desc[r], kBucket[rve_q[r]].cl, kBucket[rve_q[r]].all, smem_floats, conn,
+                        rowptr, inc, econn, icode, mslot, gnode, mrowptr);
       });
     for (auto& th : pool) th.join();
     if ((e = cudaMemcpy(ms.econn, econn.data(), et * sizeof(int2), cudaMemcpyHostToDevice)) !=
