@@ -129,6 +129,54 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // CTAs never hammer a host cache line the host is writing.
 constexpr long long kServerMaxPolls = 1LL << 26;
 
+// One attempt to claim the next published request of a ring (a few CAS
+// retries under contention): its ring index, or -1 when none is waiting.
+__device__ __forceinline__ long long server_try_claim(const ServerArgs& sa) {
+  for (int tries = 0; tries < 64; ++tries) {
+    const unsigned long long h = *reinterpret_cast<volatile unsigned long long*>(sa.head);
+    const long long t = ld_gpu(sa.tail);
+    if (static_cast<long long>(h) >= t) return -1;
+    if (atomicCAS(sa.head, h, h + 1) == h) {
+      atomicMax(sa.last_claim, global_ns());
+      return static_cast<long long>(h);
+    }
+  }
+  return -1;
+}
+
+// True when a ring holds published requests nobody has claimed yet.
+__device__ __forceinline__ bool server_pending(const ServerArgs& sa) {
+  const unsigned long long h = *reinterpret_cast<volatile unsigned long long*>(sa.head);
+  return static_cast<long long>(h) < ld_gpu(sa.tail);
+}
+
+// Copies request `idx` into shared memory. The host may reuse the ring slot
+// after `cap` requests: read it with system-scope loads (no stale L1 line).
+__device__ __forceinline__ void server_read_request(const ServerArgs& sa, long long idx,
+                                                    int* s_req, double* s_F) {
+  __threadfence_system();  // order the ring entry after the tail we saw
+  const volatile ServerReq* q = sa.ring + (idx % sa.cap);
+  s_req[0] = ld_sys(&q->rve);
+  s_req[1] = ld_sys(&q->update_coords);
+  for (int k = 0; k < 9; ++k) s_F[k] = ld_sys(&q->F[k]);
+}
+
+// Publishes the completion record of request `idx` (one thread).
+__device__ __forceinline__ void server_publish_done(const ServerArgs& sa, long long idx, int rve,
+                                                    unsigned long long t_claim) {
+  __threadfence();
+  volatile ServerDone* d = sa.done + (idx % sa.cap);
+  st_sys(&d->rve, rve);
+  st_sys(&d->status, sa.st_status[rve]);
+  st_sys(&d->steps, sa.st_steps[rve]);
+  st_sys(&d->residual, sa.st_residual[rve]);
+  for (int k = 0; k < 6; ++k) st_sys(&d->sigma[k], sa.sigma[6 * rve + k]);
+  st_sys(&d->t_claim_ns, static_cast<long long>(t_claim));
+  st_sys(&d->t_done_ns, static_cast<long long>(global_ns()));
+  __threadfence_system();
+  st_release_sys(&d->ticket_plus1, idx + 1);
+}
+
 template <typename Solve>
 __device__ void server_loop(const ServerArgs& sa, Solve solve) {
   __shared__ long long s_idx;
@@ -163,15 +211,7 @@ __device__ void server_loop(const ServerArgs& sa, Solve solve) {
         __nanosleep(2000);
       }
       atomicSub(sa.idle_ctas, 1);
-      __threadfence_system();  // order the ring entry after the tail we saw
-      if (idx >= 0) {
-        // The host may reuse this ring slot after `cap` requests: read it with
-        // volatile loads (no stale L1 line) into shared memory.
-        const volatile ServerReq* q = sa.ring + (idx % sa.cap);
-        s_req[0] = ld_sys(&q->rve);
-        s_req[1] = ld_sys(&q->update_coords);
-        for (int k = 0; k < 9; ++k) s_F[k] = ld_sys(&q->F[k]);
-      }
+      if (idx >= 0) server_read_request(sa, idx, s_req, s_F);
       s_idx = idx;
     }
     __syncthreads();
@@ -190,19 +230,7 @@ __device__ void server_loop(const ServerArgs& sa, Solve solve) {
     a.st_steps = sa.st_steps;
     a.st_residual = sa.st_residual;
     solve(a, rve);  // ends with __syncthreads()
-    if (threadIdx.x == 0) {
-      __threadfence();
-      volatile ServerDone* d = sa.done + (idx % sa.cap);
-      st_sys(&d->rve, rve);
-      st_sys(&d->status, sa.st_status[rve]);
-      st_sys(&d->steps, sa.st_steps[rve]);
-      st_sys(&d->residual, sa.st_residual[rve]);
-      for (int k = 0; k < 6; ++k) st_sys(&d->sigma[k], sa.sigma[6 * rve + k]);
-      st_sys(&d->t_claim_ns, static_cast<long long>(t_claim));
-      st_sys(&d->t_done_ns, static_cast<long long>(global_ns()));
-      __threadfence_system();
-      st_release_sys(&d->ticket_plus1, idx + 1);
-    }
+    if (threadIdx.x == 0) server_publish_done(sa, idx, rve, t_claim);
     __syncthreads();
   }
 }

@@ -893,35 +893,64 @@ double batch_bytes(int64_t nt, int64_t et, int64_t nbt, int64_t R, bool mixed) {
 
 }  // namespace
 
-struct mfg_server {
-  mfg_batch* batch = nullptr;
-  cudaStream_t stream = nullptr;   // the persistent kernel
-  cudaStream_t ctrl = nullptr;     // small copies of the published count and stop flag
-  int64_t cap = 0;
-  unsigned long long idle_ns = 0;
+// One request ring of a server: requests in host-mapped memory, the
+// published count in device memory, completion records in host-mapped
+// memory, and the host's bookkeeping per ring slot.
+struct ServerLane {
   mfg::ServerReq* ring_h = nullptr;
   long long* tail_stage = nullptr;  // pinned, one published count per ring slot
-  int32_t* stop_stage = nullptr;    // pinned
   long long* tail_d = nullptr;
-  int32_t* stop_d = nullptr;
   mfg::ServerDone* done_h = nullptr;
   unsigned long long* head_d = nullptr;
-  unsigned long long* last_d = nullptr;
-  int* ctl_d = nullptr;  // [0] idle CTAs, [1] closing
   mfg::ServerArgs args{};
-  DevArray<double> sigma, res;
-  DevArray<int32_t> st, steps;
-  int64_t tail = 0;         // ring entries published
-  int64_t oldest = 0;       // oldest ring entry not yet returned
-  int64_t next_ticket = 0;
-  int64_t launches = 0;
+  int64_t tail = 0;    // ring entries published
+  int64_t oldest = 0;  // oldest ring entry not yet returned
   std::vector<int64_t> slot_ticket;
   std::vector<double> slot_submit;
   std::vector<uint8_t> slot_returned;
+
+  void release() {
+    if (ring_h) cudaFreeHost(ring_h);
+    if (tail_stage) cudaFreeHost(tail_stage);
+    if (done_h) cudaFreeHost(done_h);
+    if (tail_d) cudaFree(tail_d);
+    if (head_d) cudaFree(head_d);
+    ring_h = nullptr;
+    tail_stage = nullptr;
+    done_h = nullptr;
+    tail_d = nullptr;
+    head_d = nullptr;
+  }
+};
+
+struct mfg_server {
+  mfg_batch* batch = nullptr;
+  cudaStream_t stream = nullptr;   // the persistent kernel
+  cudaStream_t ctrl = nullptr;     // small copies of the published counts and stop flag
+  int64_t cap = 0;
+  unsigned long long idle_ns = 0;
+  // lane 0 serves RVEs solved by one CTA; lane 1, when present, the RVEs the
+  // mixed serving kernel solves with 4-CTA clusters
+  std::vector<ServerLane> lanes;
+  std::vector<uint8_t> lane_of;     // per RVE
+  int32_t* stop_stage = nullptr;    // pinned
+  int32_t* stop_d = nullptr;
+  unsigned long long* last_d = nullptr;
+  int* ctl_d = nullptr;  // [0] idle CTAs (or clusters), [1] closing
+  DevArray<double> sigma, res;
+  DevArray<int32_t> st, steps;
+  int64_t next_ticket = 0;
+  int64_t launches = 0;
   std::vector<uint8_t> busy;
   std::vector<std::deque<PendingReq>> held;
   int64_t n_held = 0;
   bool launched = false;
+
+  int64_t in_flight() const {
+    int64_t n = n_held;
+    for (const ServerLane& l : lanes) n += l.tail - l.oldest;
+    return n;
+  }
 
   ~mfg_server() {
     if (batch) cudaSetDevice(batch->device);
@@ -935,13 +964,9 @@ struct mfg_server {
       cudaStreamDestroy(stream);
     }
     if (ctrl) cudaStreamDestroy(ctrl);
-    if (ring_h) cudaFreeHost(ring_h);
-    if (tail_stage) cudaFreeHost(tail_stage);
+    for (ServerLane& l : lanes) l.release();
     if (stop_stage) cudaFreeHost(stop_stage);
-    if (done_h) cudaFreeHost(done_h);
-    if (tail_d) cudaFree(tail_d);
     if (stop_d) cudaFree(stop_d);
-    if (head_d) cudaFree(head_d);
     if (last_d) cudaFree(last_d);
     if (ctl_d) cudaFree(ctl_d);
     sigma.release();
@@ -963,10 +988,11 @@ mfg_status server_ensure_running(mfg_server* sv) {
   }
   // a fresh kernel starts with no CTA waiting and the closing flag down
   MFG_CUDA(cudaMemsetAsync(sv->ctl_d, 0, 2 * sizeof(int), sv->stream));
+  const mfg::ServerArgs* big = sv->lanes.size() > 1 ? &sv->lanes[1].args : nullptr;
   cudaError_t e = sv->batch->precision == MFG_PREC_MIXED
-                      ? mfg::launch_server_mixed(*sv->batch->mixed, sv->batch->dev, sv->args,
-                                                 sv->stream)
-                      : mfg::launch_server_f64(sv->batch->dev, sv->args,
+                      ? mfg::launch_server_mixed(*sv->batch->mixed, sv->batch->dev,
+                                                 sv->lanes[0].args, big, sv->stream)
+                      : mfg::launch_server_f64(sv->batch->dev, sv->lanes[0].args,
                                                sv->batch->sms * mfg::relax_f64_max_blocks_per_sm(0),
                                                sv->stream);
   if (e != cudaSuccess) return fail(MFG_E_CUDA, "serving launch failed: %s", cudaGetErrorString(e));
@@ -975,25 +1001,60 @@ mfg_status server_ensure_running(mfg_server* sv) {
   return MFG_OK;
 }
 
-// Writes one request into the ring and publishes it: the entry is stored
-// first, then the new published count is copied into device memory on the
-// control stream, where the CTAs poll it.
+// Writes one request into its RVE's ring and publishes it: the entry is
+// stored first, then the new published count is copied into device memory
+// on the control stream, where the kernel polls it.
 mfg_status server_publish(mfg_server* sv, int32_t rve, const PendingReq& p) {
-  const int64_t idx = sv->tail;
-  mfg::ServerReq& q = sv->ring_h[idx % sv->cap];
+  ServerLane& l = sv->lanes[sv->lane_of[rve]];
+  const int64_t idx = l.tail;
+  mfg::ServerReq& q = l.ring_h[idx % sv->cap];
   q.rve = rve;
   q.update_coords = p.update;
   q.ticket = p.ticket;
   for (int k = 0; k < 9; ++k) q.F[k] = p.F[k];
-  sv->slot_ticket[idx % sv->cap] = p.ticket;
-  sv->slot_submit[idx % sv->cap] = p.t_submit;
-  sv->slot_returned[idx % sv->cap] = 0;
+  l.slot_ticket[idx % sv->cap] = p.ticket;
+  l.slot_submit[idx % sv->cap] = p.t_submit;
+  l.slot_returned[idx % sv->cap] = 0;
   std::atomic_thread_fence(std::memory_order_seq_cst);
-  sv->tail = idx + 1;
-  sv->tail_stage[idx % sv->cap] = sv->tail;
+  l.tail = idx + 1;
+  l.tail_stage[idx % sv->cap] = l.tail;
   sv->busy[rve] = 1;
-  MFG_CUDA(cudaMemcpyAsync(sv->tail_d, &sv->tail_stage[idx % sv->cap], sizeof(long long),
+  MFG_CUDA(cudaMemcpyAsync(l.tail_d, &l.tail_stage[idx % sv->cap], sizeof(long long),
                            cudaMemcpyHostToDevice, sv->ctrl));
+  return MFG_OK;
+}
+
+mfg_status server_lane_create(mfg_server* sv, ServerLane& l) {
+  MFG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&l.ring_h), sv->cap * sizeof(mfg::ServerReq),
+                         cudaHostAllocMapped));
+  MFG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&l.done_h), sv->cap * sizeof(mfg::ServerDone),
+                         cudaHostAllocMapped));
+  MFG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&l.tail_stage), sv->cap * sizeof(long long),
+                         cudaHostAllocDefault));
+  MFG_CUDA(cudaMalloc(reinterpret_cast<void**>(&l.tail_d), sizeof(long long)));
+  MFG_CUDA(cudaMemset(l.tail_d, 0, sizeof(long long)));
+  std::memset(l.done_h, 0, sv->cap * sizeof(mfg::ServerDone));
+  MFG_CUDA(cudaMalloc(reinterpret_cast<void**>(&l.head_d), sizeof(unsigned long long)));
+  MFG_CUDA(cudaMemset(l.head_d, 0, sizeof(unsigned long long)));
+  mfg::ServerArgs& a = l.args;
+  MFG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(const_cast<mfg::ServerReq**>(&a.ring)),
+                                    l.ring_h, 0));
+  a.tail = l.tail_d;
+  a.stop = sv->stop_d;
+  MFG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&a.done), l.done_h, 0));
+  a.head = l.head_d;
+  a.last_claim = sv->last_d;
+  a.idle_ctas = sv->ctl_d;
+  a.closing = sv->ctl_d + 1;
+  a.cap = sv->cap;
+  a.idle_ns = sv->idle_ns;
+  a.sigma = sv->sigma.p;
+  a.st_status = sv->st.p;
+  a.st_steps = sv->steps.p;
+  a.st_residual = sv->res.p;
+  l.slot_ticket.assign(sv->cap, -1);
+  l.slot_submit.assign(sv->cap, 0.0);
+  l.slot_returned.assign(sv->cap, 1);
   return MFG_OK;
 }
 
@@ -1049,21 +1110,10 @@ mfg_status mfg_server_create(const mfg_network* nets, const mfg_strategy* strate
                                                                                    : 20000);
   MFG_CUDA(cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking));
   MFG_CUDA(cudaStreamCreateWithFlags(&sv->ctrl, cudaStreamNonBlocking));
-  MFG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&sv->ring_h), sv->cap * sizeof(mfg::ServerReq),
-                         cudaHostAllocMapped));
-  MFG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&sv->done_h), sv->cap * sizeof(mfg::ServerDone),
-                         cudaHostAllocMapped));
-  MFG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&sv->tail_stage), sv->cap * sizeof(long long),
-                         cudaHostAllocDefault));
   MFG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&sv->stop_stage), 64, cudaHostAllocDefault));
-  MFG_CUDA(cudaMalloc(reinterpret_cast<void**>(&sv->tail_d), sizeof(long long)));
   MFG_CUDA(cudaMalloc(reinterpret_cast<void**>(&sv->stop_d), sizeof(int32_t)));
-  MFG_CUDA(cudaMemset(sv->tail_d, 0, sizeof(long long)));
   MFG_CUDA(cudaMemset(sv->stop_d, 0, sizeof(int32_t)));
   *sv->stop_stage = 0;
-  std::memset(sv->done_h, 0, sv->cap * sizeof(mfg::ServerDone));
-  MFG_CUDA(cudaMalloc(reinterpret_cast<void**>(&sv->head_d), sizeof(unsigned long long)));
-  MFG_CUDA(cudaMemset(sv->head_d, 0, sizeof(unsigned long long)));
   MFG_CUDA(cudaMalloc(reinterpret_cast<void**>(&sv->last_d), sizeof(unsigned long long)));
   MFG_CUDA(cudaMemset(sv->last_d, 0, sizeof(unsigned long long)));
   MFG_CUDA(cudaMalloc(reinterpret_cast<void**>(&sv->ctl_d), 2 * sizeof(int)));
@@ -1072,25 +1122,18 @@ mfg_status mfg_server_create(const mfg_network* nets, const mfg_strategy* strate
   MFG_CUDA(sv->res.alloc(n_rve));
   MFG_CUDA(sv->st.alloc(n_rve));
   MFG_CUDA(sv->steps.alloc(n_rve));
-  mfg::ServerArgs& a = sv->args;
-  MFG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(const_cast<mfg::ServerReq**>(&a.ring)),
-                                    sv->ring_h, 0));
-  a.tail = sv->tail_d;
-  a.stop = sv->stop_d;
-  MFG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&a.done), sv->done_h, 0));
-  a.head = sv->head_d;
-  a.last_claim = sv->last_d;
-  a.idle_ctas = sv->ctl_d;
-  a.closing = sv->ctl_d + 1;
-  a.cap = sv->cap;
-  a.idle_ns = sv->idle_ns;
-  a.sigma = sv->sigma.p;
-  a.st_status = sv->st.p;
-  a.st_steps = sv->steps.p;
-  a.st_residual = sv->res.p;
-  sv->slot_ticket.assign(sv->cap, -1);
-  sv->slot_submit.assign(sv->cap, 0.0);
-  sv->slot_returned.assign(sv->cap, 1);
+  // RVEs the mixed serving kernel solves with clusters get their own ring
+  sv->lane_of.assign(n_rve, 0);
+  bool clusters = false;
+  if (b->precision == MFG_PREC_MIXED)
+    for (int r = 0; r < n_rve; ++r)
+      if (mfg::mixed_serves_in_clusters(*b->mixed, r)) {
+        sv->lane_of[r] = 1;
+        clusters = true;
+      }
+  sv->lanes.resize(clusters ? 2 : 1);
+  for (ServerLane& l : sv->lanes)
+    if ((st = server_lane_create(sv.get(), l)) != MFG_OK) return st;
   sv->busy.assign(n_rve, 0);
   sv->held.resize(n_rve);
   MFG_CUDA(cudaDeviceSynchronize());
@@ -1105,7 +1148,7 @@ mfg_status mfg_server_submit(mfg_server* sv, int32_t rve, const double* F, int32
   if (rve < 0 || rve >= sv->batch->R) return fail(MFG_E_INVALID, "rve %d out of range", rve);
   for (int k = 0; k < 9; ++k)
     if (!std::isfinite(F[k])) return fail(MFG_E_INVALID, "non-finite deformation gradient");
-  if (sv->tail - sv->oldest + sv->n_held >= sv->cap)
+  if (sv->in_flight() >= sv->cap)
     return fail(MFG_E_BUSY, "request ring full (%lld entries)", static_cast<long long>(sv->cap));
   MFG_CUDA(cudaSetDevice(sv->batch->device));
   PendingReq p;
@@ -1133,37 +1176,39 @@ mfg_status mfg_server_poll(mfg_server* sv, mfg_server_result* out, int32_t capac
   const double t_end = now_s() + 1e-3 * std::max(timeout_ms, 0);
   for (;;) {
     int32_t n = 0;
-    for (int64_t idx = sv->oldest; idx < sv->tail && n < capacity; ++idx) {
-      const int64_t slot = idx % sv->cap;
-      if (sv->slot_returned[slot]) continue;
-      const mfg::ServerDone& d = sv->done_h[slot];
-      const long long flag = *reinterpret_cast<const volatile long long*>(&d.ticket_plus1);
-      if (flag != idx + 1) continue;
-      std::atomic_thread_fence(std::memory_order_acquire);
-      mfg_server_result& r = out[n++];
-      r.ticket = sv->slot_ticket[slot];
-      r.rve = d.rve;
-      r.status = d.status;
-      r.steps = d.steps;
-      r.pad_ = 0;
-      r.residual = d.residual;
-      for (int k = 0; k < 6; ++k) r.sigma[k] = d.sigma[k];
-      r.latency_s = now_s() - sv->slot_submit[slot];
-      r.device_s = 1e-9 * static_cast<double>(d.t_done_ns - d.t_claim_ns);
-      r.t_claim_ns = d.t_claim_ns;
-      r.t_done_ns = d.t_done_ns;
-      sv->slot_returned[slot] = 1;
-      sv->busy[d.rve] = 0;
-      if (!sv->held[d.rve].empty()) {
-        PendingReq p = sv->held[d.rve].front();
-        sv->held[d.rve].pop_front();
-        sv->n_held--;
-        mfg_status st = server_publish(sv, d.rve, p);
-        if (st != MFG_OK) return st;
+    for (ServerLane& l : sv->lanes) {
+      for (int64_t idx = l.oldest; idx < l.tail && n < capacity; ++idx) {
+        const int64_t slot = idx % sv->cap;
+        if (l.slot_returned[slot]) continue;
+        const mfg::ServerDone& d = l.done_h[slot];
+        const long long flag = *reinterpret_cast<const volatile long long*>(&d.ticket_plus1);
+        if (flag != idx + 1) continue;
+        std::atomic_thread_fence(std::memory_order_acquire);
+        mfg_server_result& r = out[n++];
+        r.ticket = l.slot_ticket[slot];
+        r.rve = d.rve;
+        r.status = d.status;
+        r.steps = d.steps;
+        r.pad_ = 0;
+        r.residual = d.residual;
+        for (int k = 0; k < 6; ++k) r.sigma[k] = d.sigma[k];
+        r.latency_s = now_s() - l.slot_submit[slot];
+        r.device_s = 1e-9 * static_cast<double>(d.t_done_ns - d.t_claim_ns);
+        r.t_claim_ns = d.t_claim_ns;
+        r.t_done_ns = d.t_done_ns;
+        l.slot_returned[slot] = 1;
+        sv->busy[d.rve] = 0;
+        if (!sv->held[d.rve].empty()) {
+          PendingReq p = sv->held[d.rve].front();
+          sv->held[d.rve].pop_front();
+          sv->n_held--;
+          mfg_status st = server_publish(sv, d.rve, p);
+          if (st != MFG_OK) return st;
+        }
       }
+      while (l.oldest < l.tail && l.slot_returned[l.oldest % sv->cap]) l.oldest++;
     }
-    while (sv->oldest < sv->tail && sv->slot_returned[sv->oldest % sv->cap]) sv->oldest++;
-    const bool outstanding = sv->tail > sv->oldest || sv->n_held > 0;
+    const bool outstanding = sv->in_flight() > 0;
     if (outstanding) {
       mfg_status st = server_ensure_running(sv);
       if (st != MFG_OK) return st;
@@ -1179,9 +1224,7 @@ mfg_status mfg_server_poll(mfg_server* sv, mfg_server_result* out, int32_t capac
   }
 }
 
-int64_t mfg_server_outstanding(const mfg_server* sv) {
-  return sv ? (sv->tail - sv->oldest + sv->n_held) : 0;
-}
+int64_t mfg_server_outstanding(const mfg_server* sv) { return sv ? sv->in_flight() : 0; }
 
 int64_t mfg_server_launches(const mfg_server* sv) { return sv ? sv->launches : 0; }
 

@@ -25,9 +25,16 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
 cudaError_t run_mixed(MixedState& ms, const DevBatch& b, const RunArgs& a, cudaStream_t s,
                       int* launches);
 void mixed_destroy(MixedState* ms);
-// Persistent serving kernel on the mixed-precision solve (one CTA per SM).
-cudaError_t launch_server_mixed(MixedState& ms, const DevBatch& b, const ServerArgs& sa,
-                                cudaStream_t s);
+// Persistent serving kernel on the mixed-precision solve. Without `big`, one
+// CTA per SM serves the `small` ring; with it, 4-CTA clusters serve the
+// `big` ring (RVEs for which mixed_serves_in_clusters) as clusters and the
+// `small` ring CTA by CTA.
+cudaError_t launch_server_mixed(MixedState& ms, const DevBatch& b, const ServerArgs& small,
+                                const ServerArgs* big, cudaStream_t s);
+// Cluster size of an RVE's batch bucket, and whether the serving kernel
+// solves it as a cluster.
+int mixed_rve_cluster(const MixedState& ms, int rve);
+bool mixed_serves_in_clusters(const MixedState& ms, int rve);
 
 struct MixedStateDeleter {
   void operator()(MixedState* p) const { mixed_destroy(p); }

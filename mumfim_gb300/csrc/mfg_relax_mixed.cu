@@ -70,6 +70,8 @@ struct MixedState {
   int32_t* gnode = nullptr;    // nt
   int32_t* mrowptr = nullptr;  // nt + n_rve
   float2* mmass = nullptr;     // nt
+  int32_t* h_cl = nullptr;     // host, per RVE: cluster size of its batch bucket
+  int server_grid = 0;         // CTAs of the cluster serving kernel
   int sms = 1;
   int smem_bytes = 0;
   // Size buckets of the batch run (kBucket[q]: cluster size, force vectors
@@ -283,7 +285,7 @@ template <int CL>
 struct ClusterForces {
   uint32_t base;
   __device__ __forceinline__ float4 load(int code) const {
-    const uint32_t o = static_cast<uint32_t>(code) >> 24;
+    const uint32_t o = (static_cast<uint32_t>(code) >> 24) & 7u;
     const uint32_t a = cluster_addr(base + 8u * (static_cast<uint32_t>(code) & 0xFFFFFEu), o);
     float4 t;
     asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
@@ -827,6 +829,125 @@ server_mixed_kernel(const DevBatch b, const MixedState ms, const ServerArgs sa, 
   });
 }
 
+// Serving kernel for batches with cluster-solved RVEs: persistent 4-CTA
+// clusters. A cluster's leader (rank 0, thread 0) takes the next request of
+// the large-RVE ring and the cluster solves it together; when that ring is
+// empty and the small-RVE ring is not, the cluster's CTAs take small
+// requests one by one, each solving on its own, until the small ring runs
+// dry, a large request is waiting, or kSmallPerRound are done, and then meet
+// at one cluster barrier. Every cluster barrier is reached by all CTAs the
+// same number of times: every loop is bounded, and the decision to leave is
+// taken by the leader and broadcast before anyone acts on it. Shutdown is
+// collective as in server_loop, with clusters as the units.
+constexpr int kClusterServe = 4;
+constexpr int kSmallPerRound = 16;
+enum : int { kServeExit = 0, kServeBig = 1, kServeSmall = 2 };
+
+__global__ void __launch_bounds__(kThreadsMixed, 1)
+server_cluster_kernel(const DevBatch b, const MixedState ms, const ServerArgs big,
+                      const ServerArgs small, int smem_floats) {
+  extern __shared__ float4 smem4[];
+  float* smem = reinterpret_cast<float*>(smem4);
+  __shared__ double red[kThreadsMixed / 32 + 1];
+  __shared__ double cred[1];
+  __shared__ long long s_idx;
+  __shared__ double s_F[9];
+  __shared__ int s_req[2];
+  __shared__ int s_mode;
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = static_cast<int>(cl.block_rank());
+  const int tid = threadIdx.x;
+  const int units = static_cast<int>(gridDim.x) / kClusterServe;
+  auto args = [](const ServerArgs& sa, const double* F, int update) {
+    RunArgs a;
+    a.F = F;
+    a.n_F = 1;
+    a.update_coords = update;
+    a.sigma = sa.sigma;
+    a.st_status = sa.st_status;
+    a.st_steps = sa.st_steps;
+    a.st_residual = sa.st_residual;
+    return a;
+  };
+  for (;;) {
+    // ---- the leader picks the cluster's next job --------------------------
+    if (rank == 0 && tid == 0) {
+      int mode = kServeExit;
+      long long idx = -1;
+      const unsigned long long t0 = global_ns();
+      atomicAdd(big.idle_ctas, 1);
+      for (long long polls = 0; polls < kServerMaxPolls; ++polls) {
+        if (ld_gpu(big.stop) || ld_gpu(big.closing)) break;
+        idx = server_try_claim(big);
+        if (idx >= 0) {
+          mode = kServeBig;
+          break;
+        }
+        if (server_pending(small)) {
+          mode = kServeSmall;
+          break;
+        }
+        const unsigned long long now = global_ns();
+        const unsigned long long last =
+            *reinterpret_cast<volatile unsigned long long*>(big.last_claim);
+        const unsigned long long since = last > t0 ? last : t0;
+        if (now > since && now - since > big.idle_ns && ld_gpu(big.idle_ctas) == units) {
+          atomicExch(big.closing, 1);
+          break;
+        }
+        __nanosleep(2000);
+      }
+      atomicSub(big.idle_ctas, 1);
+      if (mode == kServeBig) server_read_request(big, idx, s_req, s_F);
+      s_mode = mode;
+      s_idx = idx;
+    }
+    cl.sync();
+    if (rank != 0) {
+      // copy the leader's decision and request into this CTA
+      if (tid == 0) s_mode = *cl.map_shared_rank(&s_mode, 0);
+      if (tid == 1) s_idx = *cl.map_shared_rank(&s_idx, 0);
+      if (tid >= 2 && tid < 4) s_req[tid - 2] = *cl.map_shared_rank(&s_req[tid - 2], 0);
+      if (tid >= 4 && tid < 13) s_F[tid - 4] = *cl.map_shared_rank(&s_F[tid - 4], 0);
+    }
+    cl.sync();
+    const int mode = s_mode;
+    if (mode == kServeExit) return;
+    if (mode == kServeBig) {
+      const long long idx = s_idx;
+      const int rve = s_req[0];
+      const unsigned long long t_claim = global_ns();
+      solve_rve_mixed<kClusterServe, false>(b, ms, args(big, s_F, s_req[1]), rve, red, cred, smem,
+                                            smem_floats);  // ends with a cluster barrier
+      if (rank == 0 && tid == 0) server_publish_done(big, idx, rve, t_claim);
+      cl.sync();
+      continue;
+    }
+    // ---- small requests, CTA by CTA ---------------------------------------
+    for (int k = 0; k < kSmallPerRound; ++k) {
+      if (tid == 0) {
+        long long idx = -1;
+        if (!ld_gpu(small.stop) && !ld_gpu(small.closing) && !server_pending(big))
+          idx = server_try_claim(small);
+        if (idx >= 0) server_read_request(small, idx, s_req, s_F);
+        s_idx = idx;
+      }
+      __syncthreads();
+      const long long idx = s_idx;
+      const int rve = s_req[0];
+      const int update = s_req[1];
+      __syncthreads();
+      if (idx < 0) break;
+      const unsigned long long t_claim = global_ns();
+      solve_rve_mixed<1, false>(b, ms, args(small, s_F, update), rve, red, cred, smem,
+                                smem_floats);  // ends with __syncthreads()
+      if (tid == 0) server_publish_done(small, idx, rve, t_claim);
+      __syncthreads();
+    }
+    cl.sync();
+  }
+}
+
 template <typename T>
 cudaError_t alloc(T** p, size_t n) {
   return cudaMalloc(reinterpret_cast<void**>(p), (n > 0 ? n : 1) * sizeof(T));
@@ -847,6 +968,7 @@ void mixed_destroy(MixedState* ms) {
                   static_cast<void*>(ms->fcon), static_cast<void*>(ms->nrm),
                   static_cast<void*>(ms->order), static_cast<void*>(ms->queues)})
     if (p) cudaFree(p);
+  delete[] ms->h_cl;
   for (int q = 0; q < kBuckets; ++q) {
     if (ms->side[q]) cudaStreamDestroy(ms->side[q]);
     if (ms->join[q]) cudaEventDestroy(ms->join[q]);
@@ -966,9 +1088,7 @@ void cluster_order(const RveDesc& d, int cl, bool all, int smem_floats,
       const int ic = inc[io + p];
       const int m = mslot[fo + (ic >> 1)];
       const int o = m / echunk;
-      if (all) {
-        icode[io + q] = (o << 24) | ((m - o * echunk) << 1) | (ic & 1);
-      } else if (m - o * echunk < K) {
+      if (m - o * echunk < K) {  // all of them when all
         icode[io + q] = kSmemFlag | (o << 24) | ((m - o * echunk) << 1) | (ic & 1);
       } else {
         icode[io + q] = (m << 1) | (ic & 1);
@@ -1054,15 +1174,30 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
   ms.smem_bytes = kSmemBytesMixed;
   const int smem_floats = kSmemBytesMixed / static_cast<int>(sizeof(float));
   if ((e = cudaFuncSetAttribute(server_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                kSmemBytesMixed)) != cudaSuccess)
+                                kSmemBytesMixed)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(server_cluster_kernel,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytesMixed)) !=
+          cudaSuccess)
     return e;
+  {
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = launch_config<kClusterServe, false>(
+        ms, static_cast<unsigned>(kClusterServe * sms), nullptr, attr);
+    int clusters = 0;
+    if ((e = cudaOccupancyMaxActiveClusters(&clusters, server_cluster_kernel, &cfg)) !=
+        cudaSuccess)
+      return e;
+    ms.server_grid = kClusterServe * clusters;
+  }
 
   // size buckets, each in longest-processing-time order
   std::vector<std::vector<int32_t>> bucket(kBuckets);
   std::vector<int> rve_q(desc.size());
+  ms.h_cl = new int32_t[std::max<size_t>(desc.size(), 1)];
   for (size_t r = 0; r < desc.size(); ++r) {
     rve_q[r] = bucket_of(desc[r], smem_floats);
     bucket[rve_q[r]].push_back(static_cast<int32_t>(r));
+    ms.h_cl[r] = kBucket[rve_q[r]].cl;
   }
   {
     // fiber order and codes of the cluster-solved RVEs
@@ -1133,11 +1268,24 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
   return cudaGetLastError();
 }
 
-cudaError_t launch_server_mixed(MixedState& ms, const DevBatch& b, const ServerArgs& sa,
-                                cudaStream_t s) {
-  server_mixed_kernel<<<ms.sms, kThreadsMixed, ms.smem_bytes, s>>>(b, ms, sa,
-                                                                   ms.smem_bytes / sizeof(float));
-  return cudaGetLastError();
+int mixed_rve_cluster(const MixedState& ms, int rve) { return ms.h_cl ? ms.h_cl[rve] : 1; }
+
+bool mixed_serves_in_clusters(const MixedState& ms, int rve) {
+  return mixed_rve_cluster(ms, rve) == kClusterServe;
+}
+
+cudaError_t launch_server_mixed(MixedState& ms, const DevBatch& b, const ServerArgs& small,
+                                const ServerArgs* big, cudaStream_t s) {
+  const int smem_floats = static_cast<int>(ms.smem_bytes / sizeof(float));
+  if (!big) {
+    server_mixed_kernel<<<ms.sms, kThreadsMixed, ms.smem_bytes, s>>>(b, ms, small, smem_floats);
+    return cudaGetLastError();
+  }
+  if (ms.server_grid < kClusterServe) return cudaErrorInvalidConfiguration;
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg =
+      launch_config<kClusterServe, false>(ms, static_cast<unsigned>(ms.server_grid), s, attr);
+  return cudaLaunchKernelEx(&cfg, server_cluster_kernel, b, ms, *big, small, smem_floats);
 }
 
 // One launch per non-empty size bucket, each on its own stream so that the
