@@ -854,21 +854,23 @@ server_cluster_kernel(const DevBatch b, const MixedState ms, const ServerArgs bi
   __shared__ double s_F[9];
   __shared__ int s_req[2];
   __shared__ int s_mode;
+  __shared__ RunArgs s_args;  // read by the solves where needed, not held in registers
   cg::cluster_group cl = cg::this_cluster();
   const int rank = static_cast<int>(cl.block_rank());
   const int tid = threadIdx.x;
   const int units = static_cast<int>(gridDim.x) / kClusterServe;
-  auto args = [](const ServerArgs& sa, const double* F, int update) {
-    RunArgs a;
-    a.F = F;
-    a.n_F = 1;
-    a.update_coords = update;
-    a.sigma = sa.sigma;
-    a.st_status = sa.st_status;
-    a.st_steps = sa.st_steps;
-    a.st_residual = sa.st_residual;
-    return a;
-  };
+  // Both rings share the per-RVE result arrays, so one RunArgs serves both;
+  // only update_coords changes per request.
+  if (tid == 0) {
+    s_args.F = s_F;
+    s_args.n_F = 1;
+    s_args.update_coords = 0;
+    s_args.sigma = big.sigma;
+    s_args.st_status = big.st_status;
+    s_args.st_steps = big.st_steps;
+    s_args.st_residual = big.st_residual;
+  }
+  __syncthreads();
   for (;;) {
     // ---- the leader picks the cluster's next job --------------------------
     if (rank == 0 && tid == 0) {
@@ -917,7 +919,9 @@ server_cluster_kernel(const DevBatch b, const MixedState ms, const ServerArgs bi
       const long long idx = s_idx;
       const int rve = s_req[0];
       const unsigned long long t_claim = global_ns();
-      solve_rve_mixed<kClusterServe, false>(b, ms, args(big, s_F, s_req[1]), rve, red, cred, smem,
+      if (tid == 0) s_args.update_coords = s_req[1];
+      __syncthreads();
+      solve_rve_mixed<kClusterServe, false>(b, ms, s_args, rve, red, cred, smem,
                                             smem_floats);  // ends with a cluster barrier
       if (rank == 0 && tid == 0) server_publish_done(big, idx, rve, t_claim);
       cl.sync();
@@ -929,17 +933,19 @@ server_cluster_kernel(const DevBatch b, const MixedState ms, const ServerArgs bi
         long long idx = -1;
         if (!ld_gpu(small.stop) && !ld_gpu(small.closing) && !server_pending(big))
           idx = server_try_claim(small);
-        if (idx >= 0) server_read_request(small, idx, s_req, s_F);
+        if (idx >= 0) {
+          server_read_request(small, idx, s_req, s_F);
+          s_args.update_coords = s_req[1];
+        }
         s_idx = idx;
       }
       __syncthreads();
       const long long idx = s_idx;
       const int rve = s_req[0];
-      const int update = s_req[1];
       __syncthreads();
       if (idx < 0) break;
       const unsigned long long t_claim = global_ns();
-      solve_rve_mixed<1, false>(b, ms, args(small, s_F, update), rve, red, cred, smem,
+      solve_rve_mixed<1, false>(b, ms, s_args, rve, red, cred, smem,
                                 smem_floats);  // ends with __syncthreads()
       if (tid == 0) server_publish_done(small, idx, rve, t_claim);
       __syncthreads();
