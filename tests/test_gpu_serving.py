@@ -130,3 +130,33 @@ def test_server_placements_match_clustered_batch(lib_path):
     for rec in res:
         assert rec["status"] == 0
         np.testing.assert_array_equal(rec["sigma"], ref[rec["rve"]])
+
+
+def test_cluster_lane_holds_requests_per_rve(lib_path):
+    """Two updating increments on an RVE the server solves with a cluster
+    (8,000 nodes) and on a small one, interleaved: each RVE's second request
+    waits for its first, and both end states equal two sequential batch
+    runs."""
+    import mumfim_gb300 as m
+    from mumfim_gb300 import synthetic as S
+    from mumfim_gb300.serving import RVEServer
+    nets = []
+    for i, n in enumerate((8_000, 1_200)):
+        coords, conn = S.knn_network(n, 4, S.geometry_seed(10, i))
+        nets.append(m.FiberNetwork(coords, conn, [S._linear_params(10, i)]))
+    strat = [m.SolutionStrategy.ramp(400, 0.5) for _ in nets]
+    F1 = np.eye(3) + 0.01 * np.array([[0, 1.0, 0], [0, 0, 0], [0, 0, -0.5]])
+    F2 = np.eye(3) + 0.01 * np.array([[0.5, 0, 0], [0, -0.2, 0.1], [0, 0, 0]])
+    g = m.BatchedFiberRVEAnalysisExplicit(nets, strat, precision="mixed")
+    s1, s2 = np.zeros((2, 6)), np.zeros((2, 6))
+    g.run(np.stack([F1, F1]), s1, update_coords=True)
+    g.run(np.stack([F2, F2]), s2, update_coords=True)
+    with RVEServer(nets, strat, precision="mixed") as sv:
+        t = [sv.submit(0, F1), sv.submit(1, F1), sv.submit(0, F2), sv.submit(1, F2)]
+        res = sv.drain()
+    assert len(res) == 4
+    by_ticket = {int(r["ticket"]): r for r in res}
+    for rve, (a, b) in enumerate(((t[0], t[2]), (t[1], t[3]))):
+        np.testing.assert_array_equal(by_ticket[a]["sigma"], s1[rve])
+        np.testing.assert_array_equal(by_ticket[b]["sigma"], s2[rve])
+        assert by_ticket[b]["t_claim_ns"] >= by_ticket[a]["t_done_ns"]
