@@ -113,10 +113,13 @@ typedef struct mfg_strategy {
 typedef enum mfg_precision { MFG_PREC_F64 = 0, MFG_PREC_MIXED = 1 } mfg_precision;
 
 typedef struct mfg_options {
-  int32_t precision;       /* mfg_precision */
-  int32_t device;          /* CUDA device ordinal */
-  int32_t threads_per_rve; /* CTA size; 0 = library default */
-  int32_t reserved[5];
+  int32_t precision;        /* mfg_precision */
+  int32_t device;           /* CUDA device ordinal */
+  int32_t threads_per_rve;  /* ignored: the CTA size is fixed per precision */
+  int32_t max_cluster_ctas; /* mixed precision: largest thread-block cluster an RVE
+                               may be split over (1, 2, 4 or 8; 0 = 8). 1 solves
+                               every RVE on one CTA, with the same results. */
+  int32_t reserved[4];
 } mfg_options;
 
 /* Per-RVE outcome of one solve. */

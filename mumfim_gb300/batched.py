@@ -108,10 +108,12 @@ class BatchedFiberRVEAnalysisExplicit:
     networks    sequence of network_io.FiberNetwork (reaction 0 drives the solve)
     strategies  one strategy.SolutionStrategy per network
     precision   "f64" (plain kernel, bit-identical to a serial CPU run) or "mixed"
+    max_cluster_ctas  mixed precision: largest thread-block cluster an RVE may be
+                split over (1, 2, 4 or 8; 0 = 8); results do not depend on it
     """
 
     def __init__(self, networks: Sequence, strategies: Sequence, precision: str = "f64",
-                 device: int = 0):
+                 device: int = 0, max_cluster_ctas: int = 0):
         L = load_library()
         if len(networks) != len(strategies):
             raise ValueError("There must be a solution strategy for each fiber network!")
@@ -119,6 +121,7 @@ class BatchedFiberRVEAnalysisExplicit:
         opts = _abi.mfg_options()
         opts.precision = {"f64": MFG_PREC_F64, "mixed": MFG_PREC_MIXED}[precision]
         opts.device = device
+        opts.max_cluster_ctas = max_cluster_ctas
         h = C.c_void_p()
         _check(L.mfg_batch_create(self._arr.nets, self._arr.strats, len(networks), C.byref(opts),
                                   C.byref(h)))

@@ -423,6 +423,10 @@ mfg_status mfg_batch_create(const mfg_network* nets, const mfg_strategy* strateg
   if (options) opt = *options;
   if (opt.precision != MFG_PREC_F64 && opt.precision != MFG_PREC_MIXED)
     return fail(MFG_E_INVALID, "unknown precision %d", opt.precision);
+  if (opt.max_cluster_ctas != 0 && opt.max_cluster_ctas != 1 && opt.max_cluster_ctas != 2 &&
+      opt.max_cluster_ctas != 4 && opt.max_cluster_ctas != 8)
+    return fail(MFG_E_INVALID, "max_cluster_ctas must be 0, 1, 2, 4 or 8 (got %d)",
+                opt.max_cluster_ctas);
   for (int r = 0; r < n_rve; ++r) {
     mfg_status st = check_strategy(strategies[r], r);
     if (st != MFG_OK) return st;
@@ -590,7 +594,8 @@ mfg_status mfg_batch_create(const mfg_network* nets, const mfg_strategy* strateg
   dv.queue = b->d_queue.p;
   if (b->precision == MFG_PREC_MIXED) {
     b->mixed.reset(mfg::mixed_new());
-    cudaError_t e = b->mixed ? mfg::mixed_create(*b->mixed, dv, b->desc, conn, rowptr, inc, b->sms, s)
+    cudaError_t e = b->mixed ? mfg::mixed_create(*b->mixed, dv, b->desc, conn, rowptr, inc, b->sms,
+                                                 opt.max_cluster_ctas > 0 ? opt.max_cluster_ctas : 8, s)
                              : cudaErrorMemoryAllocation;
     if (e != cudaSuccess)
       return fail(e == cudaErrorMemoryAllocation ? MFG_E_OOM : MFG_E_CUDA,

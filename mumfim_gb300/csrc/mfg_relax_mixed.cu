@@ -991,12 +991,14 @@ namespace {
 // holding the node state only, else one CTA that keeps what fits in shared
 // memory and streams the rest from global memory. Clusters of 8 are the last
 // resort: with 220 KB per CTA only 15 of them (120 SMs) are resident at once,
-// against 36 clusters of 4 (144 SMs).
-int bucket_of(const RveDesc& d, int smem_floats) {
+// against 36 clusters of 4 (144 SMs). Clusters above max_cluster CTAs are
+// not used.
+int bucket_of(const RveDesc& d, int smem_floats, int max_cluster) {
   static const int pref[] = {4, 3, 2, 1, 0};
   for (int q : pref)
-    if (cluster_floats(d.n_nodes, d.n_free, d.n_fibers, kBucket[q].cl, kBucket[q].all) <=
-        smem_floats)
+    if (kBucket[q].cl <= max_cluster &&
+        cluster_floats(d.n_nodes, d.n_free, d.n_fibers, kBucket[q].cl, kBucket[q].all) <=
+            smem_floats)
       return q;
   return kBuckets - 1;
 }
@@ -1159,7 +1161,8 @@ cudaError_t setup_bucket(MixedState& ms, int n, int q) {
 
 cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<RveDesc>& desc,
                          const std::vector<int2>& conn, const std::vector<int32_t>& rowptr,
-                         const std::vector<int32_t>& inc, int sms, cudaStream_t s) {
+                         const std::vector<int32_t>& inc, int sms, int max_cluster,
+                         cudaStream_t s) {
   cudaError_t e;
   const size_t nt = static_cast<size_t>(b.nt), et = static_cast<size_t>(b.et);
   if ((e = alloc(&ms.u_hl, 6 * nt)) != cudaSuccess) return e;
@@ -1201,7 +1204,7 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
   std::vector<int> rve_q(desc.size());
   ms.h_cl = new int32_t[std::max<size_t>(desc.size(), 1)];
   for (size_t r = 0; r < desc.size(); ++r) {
-    rve_q[r] = bucket_of(desc[r], smem_floats);
+    rve_q[r] = bucket_of(desc[r], smem_floats, max_cluster);
     bucket[rve_q[r]].push_back(static_cast<int32_t>(r));
     ms.h_cl[r] = kBucket[rve_q[r]].cl;
   }

@@ -117,3 +117,44 @@ def test_mixed_every_placement_and_cluster_size(M):
         one = w.subset([r])
         _, s1 = _solve(M, one, "mixed")
         np.testing.assert_array_equal(s1[0], s32[r])
+
+
+def test_cluster_and_single_cta_solves_agree(M):
+    """The same RVEs solved over thread-block clusters (2, 4 and 8 CTAs, with
+    all state or node state only on chip) and on one CTA each
+    (max_cluster_ctas=1): the same per-fiber and per-node arithmetic in the
+    same order, so the same bits, in RAMP mode and in RELAX mode (there the
+    step count too; only the residual's last bits may differ, since the
+    cluster sums it in per-CTA parts)."""
+    from mumfim_gb300 import synthetic as S
+    sizes = (4_000, 9_000, 20_000, 40_000)
+    nets, F = [], []
+    for i, n in enumerate(sizes):
+        coords, conn = S.knn_network(n, 4, S.geometry_seed(11, i))
+        nets.append(M.FiberNetwork(coords, conn, [S._linear_params(11, i)]))
+        F.append(np.eye(3) + (S.uniform(S.param_seed(11, i), 9) * 0.06 - 0.03).reshape(3, 3))
+    F = np.stack(F)
+    for strat in (M.SolutionStrategy.ramp(800, 0.5),
+                  M.SolutionStrategy(visc_damp_coeff=0.5, residual_tol=1e-6, max_steps=1_500)):
+        out = []
+        for mc in (0, 1):
+            g = M.BatchedFiberRVEAnalysisExplicit(nets, [strat] * len(nets), precision="mixed",
+                                                  max_cluster_ctas=mc)
+            s = np.zeros((len(nets), 6))
+            g.run(F, s)
+            out.append((s, g.last_status.copy(), g.displacements(2)))
+            g.close()
+        (s0, st0, u0), (s1, st1, u1) = out
+        np.testing.assert_array_equal(s0, s1)
+        np.testing.assert_array_equal(u0, u1)
+        np.testing.assert_array_equal(st0["steps"], st1["steps"])
+        np.testing.assert_array_equal(st0["status"], st1["status"])
+        np.testing.assert_allclose(st0["residual"], st1["residual"], rtol=1e-9)
+
+
+def test_max_cluster_ctas_is_checked(M):
+    from mumfim_gb300 import synthetic as S
+    w = S.config1(n_rve=1, n_nodes=300, steps=10)
+    with pytest.raises(M.MumfimGpuError, match="max_cluster_ctas"):
+        M.BatchedFiberRVEAnalysisExplicit(w.networks, w.strategies, precision="mixed",
+                                          max_cluster_ctas=3)
