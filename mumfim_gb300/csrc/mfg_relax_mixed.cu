@@ -533,13 +533,16 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   r.inc = b.inc + d.inc_off;
   r.rowptr = b.rowptr + d.row_off;
   r.mass = ms.mass + no;
-  if constexpr (CL > 1) {
-    float* nodes = smem;
+  if constexpr (CL > 1 || kAll) {
+    // this RVE's own fiber and node order (cluster_order)
     r.conn = ms.econn + fo;
     r.fcon = ms.fconc + fo;
     r.inc = ms.icode + d.inc_off;
     r.rowptr = ms.mrowptr + d.row_off;
     r.mass = ms.mmass + no;
+  }
+  if constexpr (CL > 1) {
+    float* nodes = smem;
     // force vectors first: all of the CTA's, or as many as fit beside the
     // node state (the rest in global memory)
     r.n = reinterpret_cast<float4*>(smem);
@@ -590,7 +593,7 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   for (int t = tid; t < n_own; t += kThreadsMixed) {
     const int i = t < nfo ? f_lo + t : g_lo + (t - nfo);
     const int li = t < nfo ? t : fchunk + (t - nfo);
-    const int64_t gi = CL > 1 ? __ldg(ms.gnode + no + i) : no + i;  // batch node index
+    const int64_t gi = (CL > 1 || kAll) ? __ldg(ms.gnode + no + i) : no + i;  // batch node index
     double xo[3], up[3], X[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -732,7 +735,7 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   for (int t = tid; t < n_own; t += kThreadsMixed) {
     const int i = t < nfo ? f_lo + t : g_lo + (t - nfo);
     const int li = t < nfo ? t : fchunk + (t - nfo);
-    const int64_t gi = CL > 1 ? __ldg(ms.gnode + no + i) : no + i;  // batch node index
+    const int64_t gi = (CL > 1 || kAll) ? __ldg(ms.gnode + no + i) : no + i;  // batch node index
     const NodeRec nr = load_rec(own.rec(li));
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -1032,7 +1035,7 @@ void cluster_order(const RveDesc& d, int cl, bool all, int smem_floats,
                    std::vector<int32_t>& mrowptr) {
   const int N = d.n_nodes, E = d.n_fibers, NF = d.n_free, NB = d.n_nodes - d.n_free;
   const int64_t fo = d.fiber_off, io = d.inc_off, no = d.node_off, ro = d.row_off;
-  if (cl == 1) {
+  if (cl == 1 && !all) {
     for (int e = 0; e < E; ++e) {
       mslot[fo + e] = e;
       econn[fo + e] = conn[fo + e];
@@ -1058,23 +1061,30 @@ void cluster_order(const RveDesc& d, int cl, bool all, int smem_floats,
   const int K = all ? echunk : hybrid_slots(fchunk + bchunk, echunk, smem_floats);
   auto on_chip = [&](int m, int o) { return m / echunk == o && m - o * echunk < K; };
   // nodes: position of each node (identity but for the free blocks, where
-  // nodes with only on-chip local force vectors go first)
+  // nodes with only on-chip local force vectors go first, and within each
+  // group the nodes of fewer incident fibers: the lanes of a warp then run
+  // gather loops of nearly the same length; +6 % for single CTAs)
   std::vector<int> pos(N);
   for (int j = 0; j < N; ++j) pos[j] = j;
-  {
-    for (int o = 0; o < cl; ++o) {
-      const int f_lo = std::min(NF, o * fchunk), f_hi = std::min(NF, f_lo + fchunk);
-      std::vector<int> local, cut;
-      for (int j = f_lo; j < f_hi; ++j) {
-        bool own = true;
-        for (int p = rowptr[ro + j]; p < rowptr[ro + j + 1] && own; ++p)
-          own = on_chip(mslot[fo + (inc[io + p] >> 1)], o);
-        (own ? local : cut).push_back(j);
-      }
-      int q = f_lo;
-      for (int j : local) pos[j] = q++;
-      for (int j : cut) pos[j] = q++;
+  for (int o = 0; o < cl; ++o) {
+    const int f_lo = std::min(NF, o * fchunk), f_hi = std::min(NF, f_lo + fchunk);
+    std::vector<std::pair<int, int>> order;  // (group * 1024 + degree, node)
+    order.reserve(f_hi - f_lo);
+    for (int j = f_lo; j < f_hi; ++j) {
+      bool own = true;
+      for (int p = rowptr[ro + j]; p < rowptr[ro + j + 1] && own; ++p)
+        own = on_chip(mslot[fo + (inc[io + p] >> 1)], o);
+      // (degree order only where all force vectors are on chip: with some in
+      // L2 it scatters the warps' global loads and costs more than it saves)
+      const int deg = all ? std::min(rowptr[ro + j + 1] - rowptr[ro + j], 1023) : 0;
+      order.emplace_back((own ? 0 : 1024) + deg, j);
     }
+    std::stable_sort(order.begin(), order.end(),
+                     [](const std::pair<int, int>& x, const std::pair<int, int>& y) {
+                       return x.first < y.first;
+                     });
+    int q = f_lo;
+    for (const auto& kv : order) pos[kv.second] = q++;
   }
   auto code = [&](int j) {
     const int o = owner(j);
@@ -1096,7 +1106,9 @@ void cluster_order(const RveDesc& d, int cl, bool all, int smem_floats,
       const int ic = inc[io + p];
       const int m = mslot[fo + (ic >> 1)];
       const int o = m / echunk;
-      if (m - o * echunk < K) {  // all of them when all
+      if (cl == 1) {
+        icode[io + q] = (m << 1) | (ic & 1);  // one CTA: plain positions
+      } else if (m - o * echunk < K) {  // all of them when all
         icode[io + q] = kSmemFlag | (o << 24) | ((m - o * echunk) << 1) | (ic & 1);
       } else {
         icode[io + q] = (m << 1) | (ic & 1);
