@@ -465,6 +465,51 @@ __device__ __forceinline__ float fiber_pass(const Rve& r, const Nodes& u, int e_
   return lmin;
 }
 
+// Stress of one RVE (BatchedFiberRVEAnalysisExplicitBase.h:58-126) in FP64
+// by one CTA, and its status record. Each Voigt component is a pass over the
+// boundary nodes: each thread sums a strided share in the reference's
+// boundary order, then a fixed-order block reduction. The FP64 kernel keeps
+// the reference's serial sum; here any fixed order will do, and it keeps the
+// result independent of what else runs. One component at a time keeps one
+// accumulator live.
+__device__ __forceinline__ void mixed_stress(const DevBatch& b, const RunArgs& a, int rve,
+                                             int status, int step, double residual, double* red,
+                                             bool leader) {
+  const RveDesc& d = b.desc[rve];
+  const int tid = threadIdx.x;
+  const int64_t no = d.node_off, nt = b.nt;
+  const int32_t* bo = b.bnd + d.bnd_off;
+  const int nb = leader ? d.n_nodes - d.n_free : 0;  // every CTA reduces, one sums
+  const double sc = d.scale / b.vol[rve];
+  bool bad = false;
+#pragma unroll 1
+  for (int k = 0; k < 6; ++k) {
+    // component k: (i, j) index pair of the symmetric part x_i f_j
+    const int ci = k < 3 ? k : (k == 3 ? 1 : 0);
+    const int cj = k < 3 ? k : (k == 5 ? 1 : 2);
+    const double* xi = b.x + ci * nt + no;
+    const double* xj = b.x + cj * nt + no;
+    const double* fi = b.fint + ci * nt + no;
+    const double* fj = b.fint + cj * nt + no;
+    double acc = 0.0;
+    for (int q = tid; q < nb; q += kThreadsMixed) {
+      const int i = bo[q];
+      acc += k < 3 ? xi[i] * fi[i] : 0.5 * (xi[i] * fj[i] + xj[i] * fi[i]);
+    }
+    const double sk = block_sum<kThreadsMixed>(acc, red) * sc;
+    bad = bad || !isfinite(sk);
+    if (leader && tid == 0) {
+      a.sigma[6 * rve + k] = sk;
+      if (a.update_coords) b.cur_stress[6 * rve + k] = sk;
+    }
+  }
+  if (leader && tid == 0) {
+    a.st_status[rve] = bad ? 4 : status;
+    a.st_steps[rve] = step;
+    a.st_residual[rve] = residual;
+  }
+}
+
 // Shared-memory floats of an RVE solved by a cluster of CL CTAs: 9 per node
 // slot of a CTA (displacement hi, lo and velocity; ceil(NF/CL) free plus
 // ceil(NB/CL) boundary slots), plus 4 per fiber slot (ceil(E/CL)) when the
@@ -753,39 +798,7 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
     }
   }
   Ops::sync();
-  if (rank == 0 && tid < 6) {
-    double s = 0.0;
-    const int k = tid;
-    const int32_t* bo = b.bnd + d.bnd_off;
-    const double* x0 = b.x + no;
-    const double* x1 = b.x + nt + no;
-    const double* x2 = b.x + 2 * nt + no;
-    for (int q = 0; q < N - NF; ++q) {
-      const int i = bo[q];
-      const double f1 = b.fint[no + i], f2 = b.fint[nt + no + i], f3 = b.fint[2 * nt + no + i];
-      const double crd1 = x0[i], crd2 = x1[i], crd3 = x2[i];
-      double t;
-      switch (k) {
-        case 0: t = crd1 * f1; break;
-        case 1: t = crd2 * f2; break;
-        case 2: t = crd3 * f3; break;
-        case 3: t = 0.5 * (crd2 * f3 + crd3 * f2); break;
-        case 4: t = 0.5 * (crd1 * f3 + crd3 * f1); break;
-        default: t = 0.5 * (crd1 * f2 + crd2 * f1); break;
-      }
-      s += t;
-    }
-    s *= d.scale / b.vol[rve];
-    a.sigma[6 * rve + k] = s;
-    if (a.update_coords) b.cur_stress[6 * rve + k] = s;
-    if (!isfinite(s)) status = 4;
-  }
-  const unsigned bad = __ballot_sync(0xffffffffu, tid < 32 && status == 4);
-  if (rank == 0 && tid == 0) {
-    a.st_status[rve] = bad ? 4 : status;
-    a.st_steps[rve] = step;
-    a.st_residual[rve] = residual;
-  }
+  mixed_stress(b, a, rve, status, step, residual, red, rank == 0);
   Ops::sync();
 }
 
