@@ -4,9 +4,9 @@
 // Same algorithm and step structure as the plain FP64 kernel
 // (mfg_relax_f64.cu; reference: BatchedFiberRVEAnalysisExplicitTeamOuterLoop.h:180-437),
 // with these precision choices:
-//  - positions are the FP64 reference X plus an FP32 displacement u_hi with
-//    an FP32 compensation u_lo (TwoSum / Kahan), so increments far below an
-//    FP32 ulp of u still accumulate: u = u_hi + u_lo to ~1e-14;
+//  - positions are the FP64 reference X plus an FP32 displacement hi with an
+//    FP32 compensation lo (TwoSum), so increments far below an FP32 ulp of u
+//    still accumulate: u = hi + lo to ~1e-14;
 //  - fiber forces use the Green strain formed from the displacement
 //    difference, g = (dX.du + du.du/2) / l0^2, which keeps its relative
 //    precision at small strain (the length-ratio form 0.5(l^2/l0^2 - 1)
@@ -16,21 +16,22 @@
 //    accumulated with TwoSum: recomputing u0 + alpha d in FP32 every step
 //    jitters boundary nodes by ~ulp(d), which the very short fibers kNN
 //    networks attach to the boundary turn into large strain noise;
-//  - velocities, the damping force and both kicks are FP32;
-//  - FP64 is kept for the critical time step (FP64 lengths every 100 steps),
-//    the residual norm, and the stress homogenisation, exactly where the
-//    reference reduces over the whole RVE.
-// The persistent FP64 state of the batch (x, u, volume) is read at the
-// start and written at the end of every run, so both precisions share it.
+//  - velocities, the damping force, both kicks and the critical time step's
+//    lengths (l0 sqrt(1 + 2g)) are FP32;
+//  - FP64 is kept for the residual norm and the stress homogenisation, where
+//    the reference reduces over the whole RVE, and for the persistent state
+//    of the batch (x, u, volume), read at the start and written at the end
+//    of every run, so both precisions share it.
 //
-// Memory placement, chosen per RVE inside one persistent launch (one CTA of
-// 512 threads per SM, up to 220 KB of dynamic shared memory):
-//   RESIDENT_ALL  u_hi, u_lo (24 B/node) and the per-fiber force vectors
-//                 (16 B/fiber) live in shared memory for the whole solve;
-//   RESIDENT_NODE only u_hi, u_lo in shared memory, force vectors in global;
-//   STREAM        everything in global memory (L2 / HBM).
-// Per-fiber constants (end nodes, reference vector dX, 1/l0) and per-node
-// constants / velocities always stream from global with coalesced loads.
+// Placement: one CTA of 1024 threads per SM with 220 KB of dynamic shared
+// memory. An RVE is solved by one CTA or by the 2, 4 or 8 CTAs of a
+// thread-block cluster, in size buckets launched concurrently; each CTA
+// keeps its nodes' records (hi, lo) and velocities and, where they fit, its
+// fibers' force vectors in shared memory, reading other CTAs' through
+// distributed shared memory. Cluster-solved and all-on-chip RVEs get their
+// own fiber and node order (cluster_order) that keeps most loads local and
+// the warps' work even. The largest RVEs and the serving kernels' single-CTA
+// solves place by size at run time, down to global memory.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
