@@ -55,19 +55,21 @@ struct MixedState {
   float2* mass = nullptr;  // nt, (1 / m, m)
   float4* fcon = nullptr;  // et, (X[n2] - X[n1], 1 / l0) rounded to FP32
   float4* nrm = nullptr;   // et, per-fiber force vectors (scratch; w unused)
-  // Cluster-solved RVEs have their own fiber order (see cluster_order): per
-  // fiber position the two end nodes as (owner CTA << 24 | local record) and
-  // the read-only data, per CSR incidence the force vector as (owner CTA << 24
-  // | local position << 1 | end), or (position << 1 | end) when the force
-  // vectors are in global memory. Single-CTA RVEs use the batch's own order,
-  // node ids and incidence codes.
+  // Cluster-solved and all-on-chip RVEs have their own fiber order (see
+  // cluster_order): per fiber position the two end nodes as (owner CTA << 24
+  // | local record) and the read-only data, per CSR incidence the force
+  // vector as (flag | owner CTA << 24 | local position << 1 | end) when it is
+  // in a CTA's shared memory, else (position << 1 | end). The runtime-
+  // placement solve (largest RVEs, serving kernels' single-CTA requests)
+  // uses the batch's own order, node ids and incidence codes.
   int2* econn = nullptr;      // et
   float4* fconc = nullptr;    // et
   int32_t* icode = nullptr;   // 2 * et
   int32_t* mslot = nullptr;   // et, position of each fiber slot in that order
-  // Their nodes: each CTA's free nodes whose force vectors are all its own
-  // come first (all-on-chip buckets); gnode maps a node position to the
-  // batch node index, and the CSR rows and masses follow the positions.
+  // Their nodes: each CTA's free nodes whose force vectors are all in its
+  // shared memory come first, ordered by degree in the all-on-chip buckets;
+  // gnode maps a node position to the batch node index, and the CSR rows and
+  // masses follow the positions.
   int32_t* gnode = nullptr;    // nt
   int32_t* mrowptr = nullptr;  // nt + n_rve
   float2* mmass = nullptr;     // nt
