@@ -158,3 +158,38 @@ def test_max_cluster_ctas_is_checked(M):
     with pytest.raises(M.MumfimGpuError, match="max_cluster_ctas"):
         M.BatchedFiberRVEAnalysisExplicit(w.networks, w.strategies, precision="mixed",
                                           max_cluster_ctas=3)
+
+
+@pytest.mark.parametrize("precision", ["f64", "mixed"])
+def test_degenerate_networks_match_oracle(M, oracle, precision):
+    """Networks at the edges of the set-up: every node on the boundary (no
+    free node: the solve only moves the boundary), no boundary node (the
+    RAMP increments move nothing), and a two-node, one-fiber RVE. FP64 is
+    bit-identical to the oracle; mixed agrees within 1e-5 of the largest
+    stress component (or 1e-12 absolute when the stress is zero)."""
+    from mumfim_gb300.network_io import FiberNetwork, Reaction
+    r = [Reaction(0, 1e-3, 1.0, 1.0)]
+    all_bnd = FiberNetwork(np.array([[-0.5, -0.5, 0.1], [0.5, -0.2, 0.3], [0.1, 0.5, -0.5],
+                                     [-0.2, 0.3, 0.5]]),
+                           np.array([[0, 1], [1, 2], [2, 3], [3, 0], [0, 2]], dtype=np.int32), r)
+    no_bnd = FiberNetwork(np.array([[0.0, 0.0, 0.0], [0.2, 0.0, 0.0], [0.1, 0.15, 0.0],
+                                    [0.1, 0.05, 0.2]]),
+                          np.array([[0, 1], [1, 2], [2, 0], [0, 3], [1, 3], [2, 3]],
+                                   dtype=np.int32), r)
+    pair = FiberNetwork(np.array([[-0.5, 0.0, 0.0], [0.5, 0.1, 0.0]]),
+                        np.array([[0, 1]], dtype=np.int32), r)
+    nets = [all_bnd, no_bnd, pair]
+    strat = [M.SolutionStrategy.ramp(50, 0.5) for _ in nets]
+    F = np.repeat((np.eye(3) + 0.02 * np.array([[1.0, 0.3, 0], [0, -0.5, 0], [0.1, 0, 0.2]]))[None],
+                  3, 0)
+    g = M.BatchedFiberRVEAnalysisExplicit(nets, strat, precision=precision)
+    s = np.zeros((3, 6))
+    g.run(F, s)
+    rc, so, _ = oracle.OracleBatch(nets, strat).run(F)
+    assert (g.last_status["status"] == 0).all()
+    if precision == "f64":
+        np.testing.assert_array_equal(s, so)
+    else:
+        for k in range(3):
+            scale = np.abs(so[k]).max()
+            assert np.abs(s[k] - so[k]).max() <= max(1e-5 * scale, 1e-12), (k, s[k], so[k])
