@@ -87,6 +87,13 @@ struct MixedState {
   cudaStream_t side[6] = {};
   cudaEvent_t fork = nullptr;
   cudaEvent_t join[6] = {};
+  // The batch run as a CUDA graph (queue reset, fork, one launch per bucket,
+  // join), captured for the last run arguments and replayed while they stay
+  // the same.
+  cudaStream_t capture = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  RunArgs graph_args{};
+  int graph_launches = 0;
 };
 
 namespace {
@@ -994,6 +1001,8 @@ void mixed_destroy(MixedState* ms) {
                   static_cast<void*>(ms->order), static_cast<void*>(ms->queues)})
     if (p) cudaFree(p);
   delete[] ms->h_cl;
+  if (ms->graph) cudaGraphExecDestroy(ms->graph);
+  if (ms->capture) cudaStreamDestroy(ms->capture);
   for (int q = 0; q < kBuckets; ++q) {
     if (ms->side[q]) cudaStreamDestroy(ms->side[q]);
     if (ms->join[q]) cudaEventDestroy(ms->join[q]);
@@ -1291,6 +1300,7 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
       return e;
   }
   if ((e = cudaEventCreateWithFlags(&ms.fork, cudaEventDisableTiming)) != cudaSuccess) return e;
+  if ((e = cudaStreamCreateWithFlags(&ms.capture, cudaStreamNonBlocking)) != cudaSuccess) return e;
 
   const int64_t n = std::max<int64_t>(b.nt, 1);
   mixed_prepare_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(b, ms);
@@ -1325,11 +1335,13 @@ cudaError_t launch_server_mixed(MixedState& ms, const DevBatch& b, const ServerA
   return cudaLaunchKernelEx(&cfg, server_cluster_kernel, b, ms, *big, small, smem_floats);
 }
 
+namespace {
+
 // One launch per non-empty size bucket, each on its own stream so that the
 // buckets run concurrently: the largest clusters are launched first, and the
 // CTAs of the later buckets take over SMs as the earlier buckets drain.
-cudaError_t run_mixed(MixedState& ms, const DevBatch& b, const RunArgs& a, cudaStream_t s,
-                      int* launches) {
+cudaError_t enqueue_buckets(MixedState& ms, const DevBatch& b, const RunArgs& a, cudaStream_t s,
+                            int* launches) {
   cudaError_t e;
   *launches = 0;
   if ((e = cudaMemsetAsync(ms.queues, 0, kBuckets * sizeof(int32_t), s)) != cudaSuccess)
@@ -1353,6 +1365,45 @@ cudaError_t run_mixed(MixedState& ms, const DevBatch& b, const RunArgs& a, cudaS
     if ((e = cudaStreamWaitEvent(s, ms.join[q], 0)) != cudaSuccess) return e;
   }
   return cudaSuccess;
+}
+
+bool same_args(const RunArgs& x, const RunArgs& y) {
+  return x.F == y.F && x.n_F == y.n_F && x.update_coords == y.update_coords &&
+         x.sigma == y.sigma && x.st_status == y.st_status && x.st_steps == y.st_steps &&
+         x.st_residual == y.st_residual;
+}
+
+}  // namespace
+
+// A run replays the captured graph when the arguments (device pointers and
+// flags) are those it was captured with; otherwise the bucket launches are
+// captured on a private stream into a new graph first.
+cudaError_t run_mixed(MixedState& ms, const DevBatch& b, const RunArgs& a, cudaStream_t s,
+                      int* launches) {
+  cudaError_t e;
+  if (!ms.graph || !same_args(ms.graph_args, a)) {
+    if ((e = cudaStreamBeginCapture(ms.capture, cudaStreamCaptureModeThreadLocal)) !=
+        cudaSuccess)
+      return e;
+    int n = 0;
+    const cudaError_t ec = enqueue_buckets(ms, b, a, ms.capture, &n);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(ms.capture, &g);
+    if (ec != cudaSuccess || e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return ec != cudaSuccess ? ec : e;
+    }
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return e;
+    if (ms.graph) cudaGraphExecDestroy(ms.graph);
+    ms.graph = exec;
+    ms.graph_args = a;
+    ms.graph_launches = n;
+  }
+  *launches = ms.graph_launches;
+  return cudaGraphLaunch(ms.graph, s);
 }
 
 }  // namespace mfg
