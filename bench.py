@@ -324,6 +324,9 @@ def main():
     ap.add_argument("--serve-points", type=int, default=2048)
     ap.add_argument("--serve-steps", type=int, default=500)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--autotune", action="store_true",
+                    help="mixed: time 100-step solves under each cluster-size limit first and "
+                         "use the fastest (mumfim_gb300.autotune)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the FP64 side-by-side and the served stream")
     args = ap.parse_args()
@@ -351,9 +354,18 @@ def main():
     import mumfim_gb300 as m
 
     w, desc = build_workload(args.config, rank, args.n_rve, args.solve_steps, args.nodes)
+    tune = None
+    if args.autotune and args.precision == "mixed":
+        from mumfim_gb300.autotune import tune_cluster_limit
+        t_tune = time.perf_counter()
+        best, table = tune_cluster_limit(w.networks, w.strategies, w.F, steps=100,
+                                         device=local_rank)
+        tune = {"max_cluster_ctas": best, "seconds": round(time.perf_counter() - t_tune, 1),
+                "fiber_steps_per_s_by_limit": {str(k): v for k, v in table.items()}}
     t0 = time.perf_counter()
     gpu = m.BatchedFiberRVEAnalysisExplicit(w.networks, w.strategies, precision=args.precision,
-                                            device=local_rank)
+                                            device=local_rank,
+                                            max_cluster_ctas=tune["max_cluster_ctas"] if tune else 0)
     setup_s = time.perf_counter() - t0
     R = w.n_rve
     fiber_steps = w.total_fibers * w.steps
@@ -439,7 +451,8 @@ def main():
                    "nodes_per_gpu": w.total_nodes, "explicit_steps_per_solve": w.steps,
                    "precision": args.precision, "mode": "ramp (fixed steps, linear boundary F)",
                    "l2": f"working set > L2 ({L2_BYTES >> 20} MiB): no flush needed",
-                   "parallelism": f"rve-sharded x{world}", "setup_s": round(setup_s, 2)},
+                   "parallelism": f"rve-sharded x{world}", "setup_s": round(setup_s, 2),
+                   "autotune": tune},
         "rve_solves_per_s": world * R * args.steps / (t_ms * 1e-3),
         "e2e": {"value": e2e, "unit": "fiber-steps/s", "h2d_bytes_per_step": int(F_host.nbytes),
                 "d2h_bytes_per_step": int(sig_host.nbytes + 16 * R)},
