@@ -119,8 +119,17 @@ typedef struct mfg_options {
   int32_t max_cluster_ctas; /* mixed precision: largest thread-block cluster an RVE
                                may be split over (1, 2, 4 or 8; 0 = 8). 1 solves
                                every RVE on one CTA, with the same results. */
-  int32_t reserved[4];
+  int32_t cluster_layout;   /* mixed precision: mfg_cluster_layout. MFG_LAYOUT_SERVING
+                               places RVEs that need a cluster on clusters of 4
+                               (never 2), the size the serving kernel solves in
+                               clusters; the results are the same either way. */
+  int32_t reserved[3];
 } mfg_options;
+
+typedef enum mfg_cluster_layout {
+  MFG_LAYOUT_BATCH = 0,   /* smallest of 1, 2, 4, 8 CTAs that holds the RVE */
+  MFG_LAYOUT_SERVING = 1  /* 1, 4 or 8 CTAs (mfg_server_create uses this) */
+} mfg_cluster_layout;
 
 /* Per-RVE outcome of one solve. */
 typedef struct mfg_rve_status {

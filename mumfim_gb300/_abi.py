@@ -50,7 +50,7 @@ class mfg_strategy(C.Structure):
 class mfg_options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("device", C.c_int32),
                 ("threads_per_rve", C.c_int32), ("max_cluster_ctas", C.c_int32),
-                ("reserved", C.c_int32 * 4)]
+                ("cluster_layout", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class mfg_rve_status(C.Structure):

@@ -110,10 +110,12 @@ class BatchedFiberRVEAnalysisExplicit:
     precision   "f64" (plain kernel, bit-identical to a serial CPU run) or "mixed"
     max_cluster_ctas  mixed precision: largest thread-block cluster an RVE may be
                 split over (1, 2, 4 or 8; 0 = 8); results do not depend on it
+    serving_layout  mixed precision: RVEs that need a cluster get clusters of 4
+                (never 2), the layout the serving kernel uses; same results
     """
 
     def __init__(self, networks: Sequence, strategies: Sequence, precision: str = "f64",
-                 device: int = 0, max_cluster_ctas: int = 0):
+                 device: int = 0, max_cluster_ctas: int = 0, serving_layout: bool = False):
         L = load_library()
         if len(networks) != len(strategies):
             raise ValueError("There must be a solution strategy for each fiber network!")
@@ -122,6 +124,7 @@ class BatchedFiberRVEAnalysisExplicit:
         opts.precision = {"f64": MFG_PREC_F64, "mixed": MFG_PREC_MIXED}[precision]
         opts.device = device
         opts.max_cluster_ctas = max_cluster_ctas
+        opts.cluster_layout = 1 if serving_layout else 0
         h = C.c_void_p()
         _check(L.mfg_batch_create(self._arr.nets, self._arr.strats, len(networks), C.byref(opts),
                                   C.byref(h)))

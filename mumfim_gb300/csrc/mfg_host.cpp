@@ -427,6 +427,9 @@ mfg_status mfg_batch_create(const mfg_network* nets, const mfg_strategy* strateg
       opt.max_cluster_ctas != 4 && opt.max_cluster_ctas != 8)
     return fail(MFG_E_INVALID, "max_cluster_ctas must be 0, 1, 2, 4 or 8 (got %d)",
                 opt.max_cluster_ctas);
+  if (opt.cluster_layout != MFG_LAYOUT_BATCH && opt.cluster_layout != MFG_LAYOUT_SERVING)
+    return fail(MFG_E_INVALID, "cluster_layout must be MFG_LAYOUT_BATCH or MFG_LAYOUT_SERVING "
+                "(got %d)", opt.cluster_layout);
   for (int r = 0; r < n_rve; ++r) {
     mfg_status st = check_strategy(strategies[r], r);
     if (st != MFG_OK) return st;
@@ -594,9 +597,11 @@ mfg_status mfg_batch_create(const mfg_network* nets, const mfg_strategy* strateg
   dv.queue = b->d_queue.p;
   if (b->precision == MFG_PREC_MIXED) {
     b->mixed.reset(mfg::mixed_new());
-    cudaError_t e = b->mixed ? mfg::mixed_create(*b->mixed, dv, b->desc, conn, rowptr, inc, b->sms,
-                                                 opt.max_cluster_ctas > 0 ? opt.max_cluster_ctas : 8, s)
-                             : cudaErrorMemoryAllocation;
+    cudaError_t e =
+        b->mixed ? mfg::mixed_create(*b->mixed, dv, b->desc, conn, rowptr, inc, b->sms,
+                                     opt.max_cluster_ctas > 0 ? opt.max_cluster_ctas : 8,
+                                     opt.cluster_layout == MFG_LAYOUT_SERVING, s)
+                 : cudaErrorMemoryAllocation;
     if (e != cudaSuccess)
       return fail(e == cudaErrorMemoryAllocation ? MFG_E_OOM : MFG_E_CUDA,
                   "mixed-precision set-up failed: %s", cudaGetErrorString(e));
@@ -892,7 +897,8 @@ struct PendingReq {
 // working set when used), for admission against the HBM budget.
 double batch_bytes(int64_t nt, int64_t et, int64_t nbt, int64_t R, bool mixed) {
   double b = nt * (5 * 3 * 8.0 + 8 + 4) + et * (8.0 + 8 + 24 + 8) + nbt * (48.0 + 4) + R * 200.0;
-  if (mixed) b += nt * (24.0 + 12 + 8 + 4 + 4 + 8) + et * (16.0 + 16 + 16 + 8 + 8 + 4) + R * 12.0;
+  if (mixed)  // + node-centric incidences (about 2.3 per fiber, with the set-up fiber ids)
+    b += nt * (24.0 + 12 + 8 + 4 + 4 + 8 + 8) + et * (16.0 + 16 + 16 + 8 + 8 + 4 + 64) + R * 20.0;
   return b;
 }
 
@@ -1087,6 +1093,7 @@ mfg_status mfg_server_create(const mfg_network* nets, const mfg_strategy* strate
   mfg_default_options(&bo);
   bo.precision = opt.precision;
   bo.device = opt.device;
+  bo.cluster_layout = MFG_LAYOUT_SERVING;
   // admission: the device state of every registered RVE must fit the budget
   if (nets && n_rve > 0) {
     int64_t nt = 0, et = 0;

@@ -20,7 +20,7 @@ MixedState* mixed_new();
 cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<RveDesc>& desc,
                          const std::vector<int2>& conn, const std::vector<int32_t>& rowptr,
                          const std::vector<int32_t>& inc, int sms, int max_cluster,
-                         cudaStream_t s);
+                         bool serving_layout, cudaStream_t s);
 // One run: reads the persistent FP64 state (x, u, vol), relaxes in mixed
 // precision and writes the FP64 state, stress and status back.
 cudaError_t run_mixed(MixedState& ms, const DevBatch& b, const RunArgs& a, cudaStream_t s,

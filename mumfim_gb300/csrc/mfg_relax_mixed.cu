@@ -73,7 +73,17 @@ struct MixedState {
   int32_t* gnode = nullptr;    // nt
   int32_t* mrowptr = nullptr;  // nt + n_rve
   float2* mmass = nullptr;     // nt
+  // Node-centric RVEs: per node position its (first incidence, degree) in
+  // the RVE's SELL-32 incidence block, which starts at sell_off[rve]; per
+  // incidence the other end's code and the fiber's data (solve_rve_nodal).
+  int2* nsell = nullptr;         // nt
+  int64_t* sell_off = nullptr;   // n_rve
+  int32_t* ncode = nullptr;      // SELL elements
+  float4* nfc = nullptr;         // SELL elements
+  int64_t n_sell = 0;
+  int64_t* nfib_tmp = nullptr;   // set-up only: fiber of each SELL element
   int32_t* h_cl = nullptr;     // host, per RVE: cluster size of its batch bucket
+  int32_t* rve_bucket = nullptr;  // device, per RVE: its batch bucket (serving kernels)
   int server_grid = 0;         // CTAs of the cluster serving kernel
   int sms = 1;
   int smem_bytes = 0;
@@ -102,12 +112,20 @@ constexpr int kThreadsMixed = 1024;
 constexpr int kSmemBytesMixed = 220 * 1024;
 // Size buckets, launched in this order (largest clusters first).
 struct BucketKind {
-  int cl;    // CTAs per cluster
-  bool all;  // fiber force vectors in shared memory too
+  int cl;      // CTAs per cluster
+  bool all;    // fiber-centric: force vectors in shared memory too
+  bool nodal;  // node-centric solve (node state in shared memory)
 };
 constexpr int kBuckets = 6;
-constexpr BucketKind kBucket[kBuckets] = {{8, false}, {4, false}, {4, true},
-                                          {2, true},  {1, true},  {1, false}};
+constexpr BucketKind kBucket[kBuckets] = {{8, false, true}, {4, false, true}, {2, false, true},
+                                          {1, false, true}, {1, true, false}, {1, false, false}};
+// Placement preference (bucket_of): the first bucket whose shared memory
+// holds the RVE, else the last bucket.
+constexpr int kPref[] = {4, 3, 2, 1, 0};
+// The single-CTA buckets with an RVE order of their own, by kind.
+constexpr int kQNodal1 = 3, kQFiberAll = 4;
+static_assert(kBucket[kQNodal1].cl == 1 && kBucket[kQNodal1].nodal, "bucket table");
+static_assert(kBucket[kQFiberAll].cl == 1 && kBucket[kQFiberAll].all, "bucket table");
 
 __global__ void mixed_prepare_kernel(const DevBatch b, MixedState ms) {
   const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
@@ -136,6 +154,15 @@ __global__ void mixed_prepare_fibers_kernel(const DevBatch b, MixedState ms) {
     }
     ms.fcon[fo] = make_float4(dx[0], dx[1], dx[2], static_cast<float>(1.0 / b.l0[fo]));
     ms.fconc[d.fiber_off + ms.mslot[fo]] = ms.fcon[fo];
+  }
+}
+
+// Fiber data of the node-centric incidences (fiber -1: padding).
+__global__ void mixed_prepare_sell_kernel(const MixedState ms, const int64_t* nfib, int64_t n) {
+  const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (i < n) {
+    const int64_t e = nfib[i];
+    ms.nfc[i] = e >= 0 ? ms.fcon[e] : make_float4(0.f, 0.f, 0.f, 0.f);
   }
 }
 
@@ -215,16 +242,12 @@ __device__ __forceinline__ void split(double u, float& hi, float& lo) {
 struct Rve {
   RveDesc d;
   Law L;
-  // This CTA's fiber force vectors: position e is kept in shared memory at
-  // n[e - e_base] when e - e_base < nk, else in global memory at ng[e].
-  float4* n;
-  int e_base, nk;
-  float4* ng;
+  float4* n;            // fiber force vectors (fiber-centric solve)
   const float2* mass;   // (1 / m, m)
   const float4* fcon;   // (dX, 1 / l0)
   const int2* conn;     // end nodes (node ids, or cluster codes)
   const int32_t* rowptr;
-  const int32_t* inc;   // incidences (slot << 1 | end, or cluster codes)
+  const int32_t* inc;   // incidences (slot << 1 | end)
   float* ramp;          // per boundary node: step increment d/n as (hi[3], lo[3])
   int64_t node_off, nt;
 };
@@ -281,50 +304,11 @@ struct ClusterNodes {
   }
 };
 
-// Fiber force vectors in one CTA's shared memory or in global memory, by
+// Fiber force vectors in the CTA's shared memory or in global memory, by
 // incidence code (slot << 1 | end).
 struct LocalForces {
   const float4* p;
   __device__ __forceinline__ float4 load(int code) const { return p[code >> 1]; }
-};
-
-// Fiber force vectors of an RVE split over a cluster: CTA o holds its slots
-// as float4 at shared-memory offset 0; an incidence is given by its code
-// (owner << 24 | local slot << 1 | end).
-template <int CL>
-struct ClusterForces {
-  uint32_t base;
-  __device__ __forceinline__ float4 load(int code) const {
-    const uint32_t o = (static_cast<uint32_t>(code) >> 24) & 7u;
-    const uint32_t a = cluster_addr(base + 8u * (static_cast<uint32_t>(code) & 0xFFFFFEu), o);
-    float4 t;
-    asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
-                 : "=f"(t.x), "=f"(t.y), "=f"(t.z), "=f"(t.w)
-                 : "r"(a));
-    return t;
-  }
-};
-
-// Force vectors of an RVE whose clusters keep part of them in shared memory:
-// an incidence code with kSmemFlag set reads CTA o's shared memory at its
-// local position, any other reads global memory at its position.
-constexpr int kSmemFlag = 1 << 30;
-template <int CL>
-struct HybridForces {
-  uint32_t base;
-  const float4* g;
-  __device__ __forceinline__ float4 load(int code) const {
-    if (code & kSmemFlag) {
-      const uint32_t o = (static_cast<uint32_t>(code) >> 24) & 7u;
-      const uint32_t a = cluster_addr(base + 8u * (static_cast<uint32_t>(code) & 0xFFFFFEu), o);
-      float4 t;
-      asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
-                   : "=f"(t.x), "=f"(t.y), "=f"(t.z), "=f"(t.w)
-                   : "r"(a));
-      return t;
-    }
-    return g[code >> 1];
-  }
 };
 
 template <int CL>
@@ -426,36 +410,45 @@ __device__ __forceinline__ NodeConst load_node(const Rve& r, int i) {
 // would cancel.
 // Returns the current length l0 sqrt(1 + 2g), which the critical time step
 // needs every 100 steps (unused, and so not computed, on the other steps).
-template <bool kSplit, class Nodes>
-__device__ __forceinline__ float fiber_force(const Rve& r, const Nodes& u, int e,
-                                             const FiberConst& k) {
-  const NodeRec na = u.load(k.c.x), nb = u.load(k.c.y);
-  float du[3];
+//
+// The steps are split so that the node-centric pass (which forms the same
+// vector from either end) runs exactly the same arithmetic.
+__device__ __forceinline__ void disp_diff(const NodeRec& na, const NodeRec& nb, float du[3]) {
 #pragma unroll
   for (int q = 0; q < 3; ++q) {
     float d, ed;
     two_sum(nb.hi[q], -na.hi[q], d, ed);
     du[q] = d + (ed + (nb.lo[q] - na.lo[q]));
   }
-  const float4 fc = k.fc;
+}
+__device__ __forceinline__ float green(const float du[3], const float4& fc) {
   const float gn = fmaf(du[0], fmaf(0.5f, du[0], fc.x),
                         fmaf(du[1], fmaf(0.5f, du[1], fc.y), du[2] * fmaf(0.5f, du[2], fc.z)));
-  const float g = gn * (fc.w * fc.w);
-  const float t = tension_over_length(r.L, g, fc.w);
-  const float4 f = make_float4((fc.x + du[0]) * t, (fc.y + du[1]) * t, (fc.z + du[2]) * t, 0.f);
-  const int le = e - r.e_base;
-  if (!kSplit || le < r.nk)
-    r.n[le] = f;
-  else
-    r.ng[e] = f;
-  return sqrtf(fmaxf(fmaf(2.f, g, 1.f), 0.f)) / fc.w;
+  return gn * (fc.w * fc.w);
+}
+__device__ __forceinline__ float4 force_vec(const Law& L, const float du[3], const float4& fc,
+                                            float g) {
+  const float t = tension_over_length(L, g, fc.w);
+  return make_float4((fc.x + du[0]) * t, (fc.y + du[1]) * t, (fc.z + du[2]) * t, 0.f);
+}
+__device__ __forceinline__ float fiber_length(float g, float rl0) {
+  return sqrtf(fmaxf(fmaf(2.f, g, 1.f), 0.f)) / rl0;
+}
+
+template <class Nodes>
+__device__ __forceinline__ float fiber_force(const Rve& r, const Nodes& u, int e,
+                                             const FiberConst& k) {
+  float du[3];
+  disp_diff(u.load(k.c.x), u.load(k.c.y), du);
+  const float g = green(du, k.fc);
+  r.n[e] = force_vec(r.L, du, k.fc, g);
+  return fiber_length(g, k.fc.w);
 }
 
 // Force vectors of fiber slots e_lo + tid, + kThreadsMixed, ... < e_hi, the
 // next slot's read-only data loaded while the current one is computed.
-// Returns the shortest current length among them when kLen. kSplit: the
-// force vectors may be partly in global memory (r.nk < the CTA's count).
-template <bool kLen, bool kSplit, class Nodes>
+// Returns the shortest current length among them when kLen.
+template <bool kLen, class Nodes>
 __device__ __forceinline__ float fiber_pass(const Rve& r, const Nodes& u, int e_lo, int e_hi) {
   float lmin = FLT_MAX;
   int e = e_lo + static_cast<int>(threadIdx.x);
@@ -466,7 +459,7 @@ __device__ __forceinline__ float fiber_pass(const Rve& r, const Nodes& u, int e_
     const bool more = en < e_hi;
     FiberConst nxt = cur;
     if (more) nxt = load_fiber(r, en);
-    const float l = fiber_force<kSplit>(r, u, e, cur);
+    const float l = fiber_force(r, u, e, cur);
     if (kLen) lmin = fminf(lmin, l);
     if (!more) break;
     cur = nxt;
@@ -532,123 +525,22 @@ __host__ __device__ inline int64_t cluster_floats(int n_nodes, int n_free, int n
   return 9 * cap + (all ? 4 * echunk : 0);
 }
 
-// Force-vector slots a CTA of a node-state-only cluster keeps in shared
-// memory beside its 9 * cap floats of node state.
-__host__ __device__ inline int hybrid_slots(int cap, int echunk, int smem_floats) {
-  const int free_floats = smem_floats - 9 * cap;
-  if (free_floats <= 0) return 0;
-  return free_floats / 4 < echunk ? free_floats / 4 : echunk;
-}
-
-// One RVE solved by one CTA (CL = 1) or by the CL CTAs of a cluster. A CTA
-// of a cluster owns a contiguous range of nodes (storage order is Morton-
-// sorted, so a range is a compact region of the RVE) with their displacement
-// and velocity in its shared memory, and a range of fiber slots whose force
-// vectors it computes: in its shared memory when kAll, else in global memory.
-// A single CTA with kAll keeps everything in shared memory (the caller
-// guarantees it fits, so every shared access compiles as one); without kAll
-// it places the RVE by its size: everything in shared memory, the node state
-// only, the displacements only, or everything in global memory.
-template <int CL, bool kAll>
-__device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const RunArgs& a, int rve,
-                                double* red, double* cred, float* smem, int smem_floats) {
-  using Ops = ClusterOps<CL>;
-  Rve r;
-  r.d = b.desc[rve];
+// Prologue of a solve in FP64 for the CTA's own nodes: the affine predictor
+// (BatchedFiberRVEAnalysisExplicitBase.h:16-57) or, in RAMP mode, the
+// boundary's per-step increment; displacements split into (hi, lo); v = 0.
+// kOrder: the RVE has its own node order (gnode maps positions to nodes).
+template <bool kOrder>
+__device__ __forceinline__ void mixed_prologue(const DevBatch& b, const MixedState& ms,
+                                               const Rve& r, const double Fm[9], bool ramp,
+                                               int f_lo, int g_lo, int nfo, int n_own, int fchunk,
+                                               const LocalNodes& own, float* vel) {
   const RveDesc& d = r.d;
-  r.L = make_law(d);
-  const int N = d.n_nodes, NF = d.n_free, E = d.n_fibers;
-  const int tid = threadIdx.x;
-  const int64_t no = d.node_off, fo = d.fiber_off, nt = b.nt;
-  r.node_off = no;
-  r.nt = nt;
-  const int rank = Ops::rank();
-  const int NB = N - NF;
-  const int fchunk = (NF + CL - 1) / CL, bchunk = (NB + CL - 1) / CL, cap = fchunk + bchunk;
-  // own free nodes [f_lo, f_hi) at local index i - f_lo, own boundary nodes
-  // [g_lo, g_hi) at local index fchunk + i - g_lo (with CL = 1 both are i)
-  const int f_lo = min(NF, rank * fchunk), f_hi = min(NF, f_lo + fchunk);
-  const int g_lo = NF + min(NB, rank * bchunk), g_hi = NF + min(NB, rank * bchunk + bchunk);
-  const int nfo = f_hi - f_lo, n_own = nfo + (g_hi - g_lo);
-  const int echunk = (E + CL - 1) / CL;
-  const int e_lo = min(E, rank * echunk);
-  const int e_hi = min(E, e_lo + echunk);
-  using Nodes = std::conditional_t<(CL > 1), ClusterNodes<CL>, LocalNodes>;
-  using Forces = std::conditional_t<
-      (CL > 1), std::conditional_t<kAll, ClusterForces<CL>, HybridForces<CL>>, LocalForces>;
-  Nodes u;         // every node of the RVE (fiber pass)
-  LocalNodes own;  // the node records this CTA updates, by local index
-  float* vel;      // their velocities (x, y, z), by local index
-  Forces fv;       // every fiber force vector of the RVE (node pass)
-  r.e_base = 0;
-  r.nk = 0;
-  r.ng = ms.nrm + fo;
-  r.conn = b.conn + fo;
-  r.fcon = ms.fcon + fo;
-  r.inc = b.inc + d.inc_off;
-  r.rowptr = b.rowptr + d.row_off;
-  r.mass = ms.mass + no;
-  if constexpr (CL > 1 || kAll) {
-    // this RVE's own fiber and node order (cluster_order)
-    r.conn = ms.econn + fo;
-    r.fcon = ms.fconc + fo;
-    r.inc = ms.icode + d.inc_off;
-    r.rowptr = ms.mrowptr + d.row_off;
-    r.mass = ms.mmass + no;
-  }
-  if constexpr (CL > 1) {
-    float* nodes = smem;
-    // force vectors first: all of the CTA's, or as many as fit beside the
-    // node state (the rest in global memory)
-    r.n = reinterpret_cast<float4*>(smem);
-    r.e_base = e_lo;
-    r.nk = kAll ? echunk : hybrid_slots(cap, echunk, smem_floats);
-    fv.base = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
-    if constexpr (!kAll) fv.g = r.ng;
-    nodes = smem + 4 * r.nk;
-    u.base = static_cast<uint32_t>(__cvta_generic_to_shared(nodes));
-    own.hl = nodes;
-    vel = nodes + 6 * cap;
-  } else {
-    // force vectors first (16-byte aligned), then the node records, then the
-    // velocities
-    if (kAll || cluster_floats(N, NF, E, 1, true) <= smem_floats) {
-      r.n = reinterpret_cast<float4*>(smem);
-      r.nk = E;
-      fv.p = r.n;
-      own.hl = smem + 4 * E;
-      vel = smem + 4 * E + 6 * N;
-    } else if (cluster_floats(N, NF, E, 1, false) <= smem_floats) {
-      r.n = ms.nrm + fo;
-      fv.p = r.ng;
-      own.hl = smem;
-      vel = smem + 6 * N;
-    } else if (6LL * N <= smem_floats) {
-      r.n = ms.nrm + fo;
-      fv.p = r.ng;
-      own.hl = smem;
-      vel = ms.v + 3 * no;
-    } else {
-      r.n = ms.nrm + fo;
-      fv.p = r.ng;
-      own.hl = ms.u_hl + 6 * no;
-      vel = ms.v + 3 * no;
-    }
-    u = own;
-  }
-  r.ramp = reinterpret_cast<float*>(b.ramp + 6 * d.bnd_off);  // 12 floats per boundary node
-  const double* F = a.F + 9 * (a.n_F > 1 ? rve : 0);
-  const bool ramp = d.mode == 1;
-  double Fm[9];
-#pragma unroll
-  for (int k = 0; k < 9; ++k) Fm[k] = F[k];
-  if (a.update_coords && rank == 0 && tid == 0) b.vol[rve] = jacobian(Fm) * b.vol[rve];
-
-  // ---- prologue in FP64: predictor, split into (hi, lo), v = 0 -------------
+  const int NF = d.n_free, tid = threadIdx.x;
+  const int64_t no = d.node_off, nt = b.nt;
   for (int t = tid; t < n_own; t += kThreadsMixed) {
     const int i = t < nfo ? f_lo + t : g_lo + (t - nfo);
     const int li = t < nfo ? t : fchunk + (t - nfo);
-    const int64_t gi = (CL > 1 || kAll) ? __ldg(ms.gnode + no + i) : no + i;  // batch node index
+    const int64_t gi = kOrder ? __ldg(ms.gnode + no + i) : no + i;  // batch node index
     double xo[3], up[3], X[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -689,10 +581,103 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
       }
     }
   }
+}
+
+// RAMP mode: the own boundary nodes move by their exact (hi, lo) increment.
+__device__ __forceinline__ void ramp_boundary(const Rve& r, const LocalNodes& own, int g_lo,
+                                              int g_hi, int fchunk) {
+  const int NF = r.d.n_free;
+  for (int i = g_lo + static_cast<int>(threadIdx.x); i < g_hi; i += kThreadsMixed) {
+    const float* rb = r.ramp + 12 * (i - NF);
+    float* rec = own.rec(fchunk + (i - g_lo));
+    NodeRec nr = load_rec(rec);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float s, e;
+      two_sum(nr.hi[k], rb[k], s, e);
+      nr.hi[k] = s;
+      nr.lo[k] = nr.lo[k] + (e + rb[3 + k]);
+    }
+    store_rec(rec, nr);
+  }
+}
+
+// One RVE solved by one CTA, fiber-centric: a fiber pass forms every
+// fiber's force vector once, a node pass gathers them per node. With kAll
+// the CTA keeps everything in shared memory (the caller guarantees it fits,
+// so every shared access compiles as one) and the RVE has its own node
+// order (cluster_order); without kAll it places the RVE by its size at run
+// time, in the batch's order: everything in shared memory, the node state
+// only, the displacements only, or everything in global memory.
+template <bool kAll>
+__device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const RunArgs& a, int rve,
+                                double* red, double* cred, float* smem, int smem_floats) {
+  using Ops = ClusterOps<1>;
+  Rve r;
+  r.d = b.desc[rve];
+  const RveDesc& d = r.d;
+  r.L = make_law(d);
+  const int N = d.n_nodes, NF = d.n_free, E = d.n_fibers;
+  const int tid = threadIdx.x;
+  const int64_t no = d.node_off, fo = d.fiber_off, nt = b.nt;
+  r.node_off = no;
+  r.nt = nt;
+  // the CTA owns every node (free [0, NF), boundary [NF, N), local index =
+  // node position) and every fiber slot
+  const int rank = 0;
+  const int f_lo = 0, f_hi = NF, g_lo = NF, g_hi = N, nfo = NF, n_own = N, fchunk = NF;
+  const int e_lo = 0, e_hi = E;
+  LocalNodes own;  // the node records, by local index
+  float* vel;      // their velocities (x, y, z), by local index
+  LocalForces fv;  // every fiber force vector of the RVE (node pass)
+  r.conn = b.conn + fo;
+  r.fcon = ms.fcon + fo;
+  r.inc = b.inc + d.inc_off;
+  r.rowptr = b.rowptr + d.row_off;
+  r.mass = ms.mass + no;
+  if constexpr (kAll) {
+    // this RVE's own fiber and node order (cluster_order)
+    r.conn = ms.econn + fo;
+    r.fcon = ms.fconc + fo;
+    r.inc = ms.icode + d.inc_off;
+    r.rowptr = ms.mrowptr + d.row_off;
+    r.mass = ms.mmass + no;
+  }
+  // force vectors first (16-byte aligned), then the node records, then the
+  // velocities
+  if (kAll || cluster_floats(N, NF, E, 1, true) <= smem_floats) {
+    r.n = reinterpret_cast<float4*>(smem);
+    own.hl = smem + 4 * E;
+    vel = smem + 4 * E + 6 * N;
+  } else if (cluster_floats(N, NF, E, 1, false) <= smem_floats) {
+    r.n = ms.nrm + fo;
+    own.hl = smem;
+    vel = smem + 6 * N;
+  } else if (6LL * N <= smem_floats) {
+    r.n = ms.nrm + fo;
+    own.hl = smem;
+    vel = ms.v + 3 * no;
+  } else {
+    r.n = ms.nrm + fo;
+    own.hl = ms.u_hl + 6 * no;
+    vel = ms.v + 3 * no;
+  }
+  fv.p = r.n;
+  const LocalNodes& u = own;  // every node of the RVE (fiber pass)
+  r.ramp = reinterpret_cast<float*>(b.ramp + 6 * d.bnd_off);  // 12 floats per boundary node
+  const double* F = a.F + 9 * (a.n_F > 1 ? rve : 0);
+  const bool ramp = d.mode == 1;
+  double Fm[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Fm[k] = F[k];
+  if (a.update_coords && rank == 0 && tid == 0) b.vol[rve] = jacobian(Fm) * b.vol[rve];
+
+  // ---- prologue in FP64: predictor, split into (hi, lo), v = 0 -------------
+  mixed_prologue<kAll>(b, ms, r, Fm, ramp, f_lo, g_lo, nfo, n_own, fchunk, own, vel);
   Ops::sync();
   // critical step from the shortest current fiber (FP32 length from the
   // Green strain, ~1e-7 relative; h itself is an FP32 number)
-  const float lmin = fiber_pass<true, !kAll>(r, u, e_lo, e_hi);
+  const float lmin = fiber_pass<true>(r, u, e_lo, e_hi);
   double dt_crit =
       Ops::template combine<true>(block_min<kThreadsMixed>(lmin, red), cred) / d.sound_speed;
 
@@ -755,30 +740,16 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
         i = in;
       }
     }
-    if (ramp) {
-      for (int i = g_lo + tid; i < g_hi; i += kThreadsMixed) {
-        const float* rb = r.ramp + 12 * (i - NF);
-        float* rec = own.rec(fchunk + (i - g_lo));
-        NodeRec nr = load_rec(rec);
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          float s, e;
-          two_sum(nr.hi[k], rb[k], s, e);
-          nr.hi[k] = s;
-          nr.lo[k] = nr.lo[k] + (e + rb[3 + k]);
-        }
-        store_rec(rec, nr);
-      }
-    }
+    if (ramp) ramp_boundary(r, own, g_lo, g_hi, fchunk);
     Ops::sync();
     const bool dt_step = (step % kUpdateFreq) == 0;
     if (dt_step) {
-      const float lm = fiber_pass<true, !kAll>(r, u, e_lo, e_hi);
+      const float lm = fiber_pass<true>(r, u, e_lo, e_hi);
       dt_crit =
           Ops::template combine<true>(block_min<kThreadsMixed>(lm, red), cred) / d.sound_speed;
       h_cur = static_cast<float>(d.crit * dt_crit * 0.5);
     } else {
-      fiber_pass<false, !kAll>(r, u, e_lo, e_hi);
+      fiber_pass<false>(r, u, e_lo, e_hi);
       Ops::sync();
     }
     h_prev = h;
@@ -790,7 +761,7 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   for (int t = tid; t < n_own; t += kThreadsMixed) {
     const int i = t < nfo ? f_lo + t : g_lo + (t - nfo);
     const int li = t < nfo ? t : fchunk + (t - nfo);
-    const int64_t gi = (CL > 1 || kAll) ? __ldg(ms.gnode + no + i) : no + i;  // batch node index
+    const int64_t gi = kAll ? __ldg(ms.gnode + no + i) : no + i;  // batch node index
     const NodeRec nr = load_rec(own.rec(li));
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -812,12 +783,258 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   Ops::sync();
 }
 
+// ---- node-centric solve -----------------------------------------------------
+//
+// Each thread owns nodes and forms the force vector of every fiber incident
+// to them from the fiber's two end records, in the node's CSR order: every
+// fiber is evaluated at both of its ends (twice the fiber arithmetic) and no
+// force vector is stored. Shared memory then holds only the node state
+// (records and velocities, 9 floats per node), and a step's shared-memory
+// traffic is the end records plus the own state, against records, force
+// vector stores and force vector gathers in the fiber-centric solve above.
+// The vector of a fiber is the same bits at either end and as the fiber
+// pass forms it: the displacement difference is formed in the node's
+// direction and its sign flipped at the fiber's first end, which is exact
+// (rounding to nearest is symmetric), so both solves give the same results.
+//
+// Incidences are stored sliced by warp (SELL-32): the own nodes of a CTA, in
+// the order its threads visit them (free nodes, then boundary nodes), form
+// slices of 32, a slice as wide as its largest degree, and the k-th
+// incidence of the node at lane l of a slice is at slice base + 32 k + l. A
+// warp's loads of incidence codes and fiber data are then contiguous. An
+// incidence holds (other end's node code << 1 | 1 if this node is the
+// fiber's second end) and the fiber's (X[n2] - X[n1], 1 / l0).
+
+// Internal force of one node with record `me` from its deg incidences
+// starting at p.
+template <class Nodes>
+__device__ __forceinline__ void nodal_force(const Law& L, const Nodes& u, const int32_t* ncode,
+                                            const float4* nfc, int p, int deg, const NodeRec& me,
+                                            float& a0, float& a1, float& a2) {
+  a0 = 0.f; a1 = 0.f; a2 = 0.f;
+  if (deg <= 0) return;
+  int c = __ldg(ncode + p);
+  float4 fc = __ldg(nfc + p);
+  for (int k = 1;; ++k) {
+    const bool more = k < deg;
+    int cn = c;
+    float4 fcn = fc;
+    if (more) {
+      p += 32;
+      cn = __ldg(ncode + p);
+      fcn = __ldg(nfc + p);
+    }
+    const NodeRec o = u.load(c >> 1);
+    const float sg = (c & 1) ? 1.f : -1.f;
+    float du[3];
+    disp_diff(o, me, du);  // x_me - x_o: the fiber's du at its second end
+#pragma unroll
+    for (int q = 0; q < 3; ++q) du[q] *= sg;
+    const float g = green(du, fc);
+    const float4 f = force_vec(L, du, fc, g);
+    a0 = fmaf(sg, f.x, a0);
+    a1 = fmaf(sg, f.y, a1);
+    a2 = fmaf(sg, f.z, a2);
+    if (!more) break;
+    c = cn;
+    fc = fcn;
+  }
+}
+
+// Shortest current length among fiber slots e_lo + tid, + kThreadsMixed, ...
+// < e_hi (the critical time step's input, every 100 steps).
+template <class Nodes>
+__device__ __forceinline__ float length_pass(const Rve& r, const Nodes& u, int e_lo, int e_hi) {
+  float lmin = FLT_MAX;
+  for (int e = e_lo + static_cast<int>(threadIdx.x); e < e_hi; e += kThreadsMixed) {
+    const FiberConst k = load_fiber(r, e);
+    float du[3];
+    disp_diff(u.load(k.c.x), u.load(k.c.y), du);
+    lmin = fminf(lmin, fiber_length(green(du, k.fc), k.fc.w));
+  }
+  return lmin;
+}
+
+// One RVE by one CTA or the CL CTAs of a cluster, node-centric; every CTA
+// keeps its own nodes' records and velocities in shared memory (the caller
+// guarantees 9 floats per node slot fit). Node ranges per CTA, the node
+// order and the fiber-slot ranges (used by the length pass) are those of
+// the fiber-centric cluster solve.
+//
+// Step structure (same arithmetic and order as the fiber-centric solve):
+// on every 100th step the length pass refreshes the time step; pass A forms
+// each own free node's force, sums the residual on those steps and applies
+// the kick (v += h f / m, both half kicks in one); pass B, after a barrier,
+// drifts the own free nodes (x += 2h v) and moves the RAMP boundary.
+template <int CL>
+__device__ void solve_rve_nodal(const DevBatch& b, const MixedState& ms, const RunArgs& a, int rve,
+                                double* red, double* cred, float* smem) {
+  using Ops = ClusterOps<CL>;
+  Rve r;
+  r.d = b.desc[rve];
+  const RveDesc& d = r.d;
+  r.L = make_law(d);
+  const int N = d.n_nodes, NF = d.n_free, E = d.n_fibers;
+  const int tid = threadIdx.x;
+  const int64_t no = d.node_off, fo = d.fiber_off, nt = b.nt;
+  r.node_off = no;
+  r.nt = nt;
+  const int rank = Ops::rank();
+  const int NB = N - NF;
+  const int fchunk = (NF + CL - 1) / CL, bchunk = (NB + CL - 1) / CL, cap = fchunk + bchunk;
+  const int f_lo = min(NF, rank * fchunk), f_hi = min(NF, f_lo + fchunk);
+  const int g_lo = NF + min(NB, rank * bchunk), g_hi = NF + min(NB, rank * bchunk + bchunk);
+  const int nfo = f_hi - f_lo, n_own = nfo + (g_hi - g_lo);
+  const int echunk = (E + CL - 1) / CL;
+  const int e_lo = min(E, rank * echunk);
+  const int e_hi = min(E, e_lo + echunk);
+  using Nodes = std::conditional_t<(CL > 1), ClusterNodes<CL>, LocalNodes>;
+  Nodes u;         // every node of the RVE
+  LocalNodes own;  // the node records this CTA updates, by local index
+  own.hl = smem;
+  float* vel = smem + 6 * cap;
+  if constexpr (CL > 1)
+    u.base = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+  else
+    u = own;
+  r.conn = ms.econn + fo;
+  r.fcon = ms.fconc + fo;
+  r.ramp = reinterpret_cast<float*>(b.ramp + 6 * d.bnd_off);
+  const int2* srow = ms.nsell + no;  // by node position: (first incidence, degree)
+  const int64_t so = ms.sell_off[rve];
+  const int32_t* ncode = ms.ncode + so;
+  const float4* nfc = ms.nfc + so;
+  const float2* mass = ms.mmass + no;
+  const double* F = a.F + 9 * (a.n_F > 1 ? rve : 0);
+  const bool ramp = d.mode == 1;
+  double Fm[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Fm[k] = F[k];
+  if (a.update_coords && rank == 0 && tid == 0) b.vol[rve] = jacobian(Fm) * b.vol[rve];
+  mixed_prologue<true>(b, ms, r, Fm, ramp, f_lo, g_lo, nfo, n_own, fchunk, own, vel);
+  Ops::sync();
+  double dt_crit = Ops::template combine<true>(
+                       block_min<kThreadsMixed>(length_pass(r, u, e_lo, e_hi), red), cred) /
+                   d.sound_speed;
+
+  const int step_cap = d.max_steps;
+  const float c = static_cast<float>(d.c);
+  float h_cur = static_cast<float>(d.crit * dt_crit * 0.5);
+  int step = 0;
+  double residual = 10.0;
+  float h_prev = 0.f;
+  int status = 0;
+  for (;;) {
+    const bool res_step = step > 0 && ((step - 1) % kUpdateFreq) == 0;
+    if (!res_step && step >= step_cap) break;
+    if (res_step) {
+      // the time step from the positions after the last drift
+      dt_crit = Ops::template combine<true>(
+                    block_min<kThreadsMixed>(length_pass(r, u, e_lo, e_hi), red), cred) /
+                d.sound_speed;
+      h_cur = static_cast<float>(d.crit * dt_crit * 0.5);
+    }
+    const float h = h_cur;
+    const float hk = h_prev + h;  // trailing kick of step-1 + leading kick of step
+    // pass A: force and kick of the own free nodes, the next node's row and
+    // mass loaded while the current one is summed
+    double part = 0.0;
+    if (tid < nfo) {
+      int t = tid;
+      int2 sr = __ldg(srow + f_lo + t);
+      float2 mm = __ldg(mass + f_lo + t);
+      for (;;) {
+        const int tn = t + kThreadsMixed;
+        const bool more = tn < nfo;
+        int2 srn = sr;
+        float2 mmn = mm;
+        if (more) {
+          srn = __ldg(srow + f_lo + tn);
+          mmn = __ldg(mass + f_lo + tn);
+        }
+        float f[3];
+        nodal_force(r.L, u, ncode, nfc, sr.x, sr.y, own.load(t), f[0], f[1], f[2]);
+        if (res_step)
+          part += static_cast<double>(f[0]) * f[0] + static_cast<double>(f[1]) * f[1] +
+                  static_cast<double>(f[2]) * f[2];
+        const float mc = mm.y * c;
+        const float km = hk * mm.x;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          float w = vel[3 * t + k];
+          w = fmaf(km, -f[k] - mc * w, w);
+          vel[3 * t + k] = w;
+        }
+        if (!more) break;
+        t = tn;
+        sr = srn;
+        mm = mmn;
+      }
+    }
+    if (res_step) {
+      residual = sqrt(Ops::template combine<false>(block_sum<kThreadsMixed>(part, red), cred));
+      if (!isfinite(residual)) {
+        status = 4;
+        break;
+      }
+      if (!ramp && !(residual > d.tol)) break;
+      if (step >= step_cap) break;
+    } else {
+      Ops::sync();
+    }
+    // pass B: drift
+    const float h2 = h + h;
+    for (int t = tid; t < nfo; t += kThreadsMixed) {
+      float* rec = own.rec(t);
+      NodeRec nr = load_rec(rec);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float w = vel[3 * t + k];
+        comp_add(nr.hi[k], nr.lo[k], h2 * w);
+      }
+      store_rec(rec, nr);
+    }
+    if (ramp) ramp_boundary(r, own, g_lo, g_hi, fchunk);
+    Ops::sync();
+    h_prev = h;
+    ++step;
+  }
+  if (status == 0 && !ramp && residual > d.tol) status = 3;
+
+  // ---- finalize: FP64 positions, boundary f_int, stress ---------------------
+  for (int t = tid; t < n_own; t += kThreadsMixed) {
+    const int i = t < nfo ? f_lo + t : g_lo + (t - nfo);
+    const int li = t < nfo ? t : fchunk + (t - nfo);
+    const int64_t gi = __ldg(ms.gnode + no + i);  // batch node index
+    const NodeRec nr = own.load(li);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double Xk = b.X[k * nt + gi];
+      const double xk = Xk + (static_cast<double>(nr.hi[k]) + nr.lo[k]);
+      b.x[k * nt + gi] = xk;
+      if (a.update_coords) b.u[k * nt + gi] = xk - Xk;
+    }
+    if (i >= NF) {
+      const int2 sr = __ldg(srow + i);
+      float a0, a1, a2;
+      nodal_force(r.L, u, ncode, nfc, sr.x, sr.y, nr, a0, a1, a2);
+      b.fint[no + i] = a0;
+      b.fint[nt + no + i] = a1;
+      b.fint[2 * nt + no + i] = a2;
+    }
+  }
+  Ops::sync();
+  mixed_stress(b, a, rve, status, step, residual, red, rank == 0);
+  Ops::sync();
+}
+
 // Persistent relaxation over one size bucket: CTA (or cluster) after cluster
 // takes the next RVE of `order` (largest first) until the bucket is empty.
-template <int CL, bool kAll>
+template <int CL, bool kAll, bool kNodal>
 __global__ void __launch_bounds__(kThreadsMixed, 1)
 relax_mixed_kernel(const DevBatch b, const MixedState ms, const RunArgs a, int smem_floats,
                    const int32_t* order, int n_order, int32_t* queue) {
+  static_assert(kNodal || CL == 1, "the fiber-centric solve runs on one CTA");
   extern __shared__ float4 smem4[];
   float* smem = reinterpret_cast<float*>(smem4);
   __shared__ double red[kThreadsMixed / 32 + 1];
@@ -840,8 +1057,26 @@ relax_mixed_kernel(const DevBatch b, const MixedState ms, const RunArgs a, int s
       __syncthreads();
     }
     if (rve < 0) break;
-    solve_rve_mixed<CL, kAll>(b, ms, a, rve, red, cred, smem, smem_floats);
+    if constexpr (kNodal)
+      solve_rve_nodal<CL>(b, ms, a, rve, red, cred, smem);
+    else
+      solve_rve_mixed<kAll>(b, ms, a, rve, red, cred, smem, smem_floats);
   }
+}
+
+// One RVE solved by one CTA of a serving kernel: with the solve of its batch
+// bucket where that is a single CTA with an order of its own, else with the
+// run-time placement. Every solve gives the same bits.
+__device__ __forceinline__ void serve_one_cta(const DevBatch& b, const MixedState& ms,
+                                              const RunArgs& a, int rve, double* red, double* cred,
+                                              float* smem, int smem_floats) {
+  const int q = __ldg(ms.rve_bucket + rve);
+  if (q == kQNodal1)
+    solve_rve_nodal<1>(b, ms, a, rve, red, cred, smem);
+  else if (q == kQFiberAll)
+    solve_rve_mixed<true>(b, ms, a, rve, red, cred, smem, smem_floats);
+  else
+    solve_rve_mixed<false>(b, ms, a, rve, red, cred, smem, smem_floats);
 }
 
 __global__ void __launch_bounds__(kThreadsMixed, 1)
@@ -851,7 +1086,7 @@ server_mixed_kernel(const DevBatch b, const MixedState ms, const ServerArgs sa, 
   __shared__ double red[kThreadsMixed / 32 + 1];
   __shared__ double cred[1];
   server_loop(sa, [&](const RunArgs& a, int rve) {
-    solve_rve_mixed<1, false>(b, ms, a, rve, red, cred, smem, smem_floats);
+    serve_one_cta(b, ms, a, rve, red, cred, smem, smem_floats);
   });
 }
 
@@ -947,8 +1182,8 @@ server_cluster_kernel(const DevBatch b, const MixedState ms, const ServerArgs bi
       const unsigned long long t_claim = global_ns();
       if (tid == 0) s_args.update_coords = s_req[1];
       __syncthreads();
-      solve_rve_mixed<kClusterServe, false>(b, ms, s_args, rve, red, cred, smem,
-                                            smem_floats);  // ends with a cluster barrier
+      solve_rve_nodal<kClusterServe>(b, ms, s_args, rve, red, cred,
+                                     smem);  // ends with a cluster barrier
       if (rank == 0 && tid == 0) server_publish_done(big, idx, rve, t_claim);
       cl.sync();
       continue;
@@ -971,8 +1206,8 @@ server_cluster_kernel(const DevBatch b, const MixedState ms, const ServerArgs bi
       __syncthreads();
       if (idx < 0) break;
       const unsigned long long t_claim = global_ns();
-      solve_rve_mixed<1, false>(b, ms, s_args, rve, red, cred, smem,
-                                smem_floats);  // ends with __syncthreads()
+      serve_one_cta(b, ms, s_args, rve, red, cred, smem,
+                    smem_floats);  // ends with __syncthreads()
       if (tid == 0) server_publish_done(small, idx, rve, t_claim);
       __syncthreads();
     }
@@ -994,11 +1229,14 @@ void mixed_destroy(MixedState* ms) {
   for (void* p : {static_cast<void*>(ms->u_hl), static_cast<void*>(ms->econn),
                   static_cast<void*>(ms->icode), static_cast<void*>(ms->mslot),
                   static_cast<void*>(ms->gnode), static_cast<void*>(ms->mrowptr),
-                  static_cast<void*>(ms->mmass),
+                  static_cast<void*>(ms->mmass), static_cast<void*>(ms->nsell),
+                  static_cast<void*>(ms->sell_off), static_cast<void*>(ms->ncode),
+                  static_cast<void*>(ms->nfc), static_cast<void*>(ms->nfib_tmp),
                   static_cast<void*>(ms->fconc),
                   static_cast<void*>(ms->v), static_cast<void*>(ms->mass),
                   static_cast<void*>(ms->fcon), static_cast<void*>(ms->nrm),
-                  static_cast<void*>(ms->order), static_cast<void*>(ms->queues)})
+                  static_cast<void*>(ms->order), static_cast<void*>(ms->queues),
+                  static_cast<void*>(ms->rve_bucket)})
     if (p) cudaFree(p);
   delete[] ms->h_cl;
   if (ms->graph) cudaGraphExecDestroy(ms->graph);
@@ -1013,54 +1251,53 @@ void mixed_destroy(MixedState* ms) {
 
 namespace {
 
-// Bucket of an RVE: one CTA if all its mutable state (displacement hi, lo,
-// velocity, fiber force vectors) fits in its shared memory, else the
-// smallest cluster of 2 or 4 over which it fits, else clusters of 4, then 8,
-// holding the node state only, else one CTA that keeps what fits in shared
-// memory and streams the rest from global memory. Clusters of 8 are the last
-// resort: with 220 KB per CTA only 15 of them (120 SMs) are resident at once,
-// against 36 clusters of 4 (144 SMs). Clusters above max_cluster CTAs are
-// not used.
-int bucket_of(const RveDesc& d, int smem_floats, int max_cluster) {
-  static const int pref[] = {4, 3, 2, 1, 0};
-  for (int q : pref)
-    if (kBucket[q].cl <= max_cluster &&
-        cluster_floats(d.n_nodes, d.n_free, d.n_fibers, kBucket[q].cl, kBucket[q].all) <=
-            smem_floats)
+// Bucket of an RVE: the smallest of one CTA or a cluster of 2, 4 or 8 CTAs
+// whose shared memory holds its node state (node-centric solve), else one
+// CTA that keeps what fits in shared memory and streams the rest from global
+// memory (fiber-centric solve). Clusters of 8 are the last resort: with
+// 220 KB per CTA only 15 of them (120 SMs) are resident at once, against 36
+// clusters of 4 (144 SMs). Clusters above max_cluster CTAs are not used,
+// nor clusters of 2 in the serving layout (the serving kernel solves in
+// clusters of 4 only).
+int bucket_of(const RveDesc& d, int smem_floats, int max_cluster, bool serving_layout) {
+  for (int q : kPref)
+    if (kBucket[q].cl <= max_cluster && !(serving_layout && kBucket[q].cl == 2) &&
+        cluster_floats(d.n_nodes, d.n_free, d.n_fibers, kBucket[q].cl,
+                       kBucket[q].all && !kBucket[q].nodal) <= smem_floats)
       return q;
   return kBuckets - 1;
 }
 
-// Fiber and node order of an RVE solved by a cluster of cl CTAs.
+// Fiber and node order of an RVE with its own order: one solved by a
+// cluster of cl CTAs, or by one CTA with all its state in shared memory.
 //
 // Fibers: each goes to the CTA that owns its lower-numbered end (a free node
 // whenever the fiber has one); within a CTA, fibers with both ends owned by
 // that CTA come first, then the fibers that cross to another CTA, each group
-// in slot order. CTA o computes positions [o*echunk, (o+1)*echunk), so most
-// warps see only local end nodes: a load of about 37 cycles through the
-// cluster window against about 200 for a peer CTA's shared memory.
+// in slot order. CTA o takes fiber positions [o*echunk, (o+1)*echunk) in the
+// length pass, so most warps see only local end nodes: a load of about 37
+// cycles through the cluster window against about 200 for a peer CTA's
+// shared memory.
 //
-// Force vectors: in the node-state-only buckets a CTA keeps its first K
-// positions (K = hybrid_slots) in shared memory and the rest in global
-// memory; in the others all of them in shared memory.
-//
-// Nodes: within each CTA's block of free nodes, those whose incident force
-// vectors are all in that CTA's shared memory come first, so the gathers of
-// most warps stay local too. Boundary nodes keep their places.
+// Nodes: within each CTA's block of free nodes, those whose neighbours are
+// all owned by that CTA come first, and within each group the nodes of fewer
+// incident fibers, so the lanes of a warp run loops of nearly the same
+// length (+6 % for the fiber-centric single CTA) and the warps that wait on
+// other CTAs are few. Boundary nodes keep their places.
 //
 // Writes the fiber positions (mslot), the end-node codes by position
-// (econn), the node index by node position (gnode, batch-wide), the CSR rows
-// by node position (mrowptr) and the force-vector codes of their incidences
-// (icode). Single-CTA RVEs keep the batch's order.
-void cluster_order(const RveDesc& d, int cl, bool all, int smem_floats,
-                   const std::vector<int2>& conn,
+// (econn), the node index by node position (gnode, batch-wide), and the CSR
+// rows by node position (mrowptr) with their incidences as (fiber position
+// << 1 | end) (icode), which the single-CTA fiber-centric solve reads. RVEs
+// without their own order (own_order false) keep the batch's order.
+void cluster_order(const RveDesc& d, int cl, bool own_order, const std::vector<int2>& conn,
                    const std::vector<int32_t>& rowptr, const std::vector<int32_t>& inc,
                    std::vector<int2>& econn, std::vector<int32_t>& icode,
                    std::vector<int32_t>& mslot, std::vector<int32_t>& gnode,
                    std::vector<int32_t>& mrowptr) {
   const int N = d.n_nodes, E = d.n_fibers, NF = d.n_free, NB = d.n_nodes - d.n_free;
   const int64_t fo = d.fiber_off, io = d.inc_off, no = d.node_off, ro = d.row_off;
-  if (cl == 1 && !all) {
+  if (!own_order) {
     for (int e = 0; e < E; ++e) {
       mslot[fo + e] = e;
       econn[fo + e] = conn[fo + e];
@@ -1082,13 +1319,7 @@ void cluster_order(const RveDesc& d, int cl, bool all, int smem_floats,
   }
   for (int k = 0; k < 2 * cl; ++k) start[k + 1] += start[k];
   for (int e = 0; e < E; ++e) mslot[fo + e] = start[key[e]]++;
-  const int echunk = (E + cl - 1) / cl;
-  const int K = all ? echunk : hybrid_slots(fchunk + bchunk, echunk, smem_floats);
-  auto on_chip = [&](int m, int o) { return m / echunk == o && m - o * echunk < K; };
-  // nodes: position of each node (identity but for the free blocks, where
-  // nodes with only on-chip local force vectors go first, and within each
-  // group the nodes of fewer incident fibers: the lanes of a warp then run
-  // gather loops of nearly the same length; +6 % for single CTAs)
+  // nodes: position of each node (identity but for the free blocks)
   std::vector<int> pos(N);
   for (int j = 0; j < N; ++j) pos[j] = j;
   for (int o = 0; o < cl; ++o) {
@@ -1096,13 +1327,14 @@ void cluster_order(const RveDesc& d, int cl, bool all, int smem_floats,
     std::vector<std::pair<int, int>> order;  // (group * 1024 + degree, node)
     order.reserve(f_hi - f_lo);
     for (int j = f_lo; j < f_hi; ++j) {
-      bool own = true;
-      for (int p = rowptr[ro + j]; p < rowptr[ro + j + 1] && own; ++p)
-        own = on_chip(mslot[fo + (inc[io + p] >> 1)], o);
-      // (degree order only where all force vectors are on chip: with some in
-      // L2 it scatters the warps' global loads and costs more than it saves)
-      const int deg = all ? std::min(rowptr[ro + j + 1] - rowptr[ro + j], 1023) : 0;
-      order.emplace_back((own ? 0 : 1024) + deg, j);
+      bool local = true;
+      for (int p = rowptr[ro + j]; p < rowptr[ro + j + 1] && local; ++p) {
+        const int ic = inc[io + p];
+        const int2 c = conn[fo + (ic >> 1)];
+        local = owner((ic & 1) ? c.x : c.y) == o;
+      }
+      const int deg = std::min(rowptr[ro + j + 1] - rowptr[ro + j], 1023);
+      order.emplace_back((local ? 0 : 1024) + deg, j);
     }
     std::stable_sort(order.begin(), order.end(),
                      [](const std::pair<int, int>& x, const std::pair<int, int>& y) {
@@ -1129,18 +1361,65 @@ void cluster_order(const RveDesc& d, int cl, bool all, int smem_floats,
     gnode[no + P] = static_cast<int32_t>(no + j);
     for (int p = rowptr[ro + j]; p < rowptr[ro + j + 1]; ++p, ++q) {
       const int ic = inc[io + p];
-      const int m = mslot[fo + (ic >> 1)];
-      const int o = m / echunk;
-      if (cl == 1) {
-        icode[io + q] = (m << 1) | (ic & 1);  // one CTA: plain positions
-      } else if (m - o * echunk < K) {  // all of them when all
-        icode[io + q] = kSmemFlag | (o << 24) | ((m - o * echunk) << 1) | (ic & 1);
-      } else {
-        icode[io + q] = (m << 1) | (ic & 1);
-      }
+      icode[io + q] = (mslot[fo + (ic >> 1)] << 1) | (ic & 1);
     }
     mrowptr[ro + P + 1] = static_cast<int32_t>(q);
   }
+}
+
+// SELL-32 incidence block of a node-centric RVE (see solve_rve_nodal), from
+// its node order (gnode): for each CTA of the cluster its own nodes in the
+// order its threads visit them (free, then boundary) form slices of 32, each
+// as wide as its largest degree. Returns the block's element count; when
+// ncode is given, also fills the block (at base) and the nodes' rows.
+int64_t sell_layout(const RveDesc& d, int cl, const std::vector<int2>& conn,
+                    const std::vector<int32_t>& rowptr, const std::vector<int32_t>& inc,
+                    const std::vector<int32_t>& gnode, int64_t base, int2* nsell, int32_t* ncode,
+                    int64_t* nfib) {
+  const int N = d.n_nodes, NF = d.n_free, NB = N - NF;
+  const int64_t no = d.node_off, ro = d.row_off, io = d.inc_off, fo = d.fiber_off;
+  const int fchunk = (NF + cl - 1) / cl, bchunk = (NB + cl - 1) / cl;
+  std::vector<int> pos;
+  if (ncode) {
+    pos.resize(N);
+    for (int P = 0; P < N; ++P) pos[gnode[no + P] - no] = P;
+  }
+  // code of the node at position P: (owner CTA << 24) | local record
+  auto code_of = [&](int P) {
+    if (P < NF) {
+      const int o = P / fchunk;
+      return (o << 24) | (P - o * fchunk);
+    }
+    const int o = (P - NF) / bchunk;
+    return (o << 24) | (fchunk + (P - NF) - o * bchunk);
+  };
+  int64_t q = 0;
+  for (int o = 0; o < cl; ++o) {
+    const int f_lo = std::min(NF, o * fchunk), f_hi = std::min(NF, f_lo + fchunk);
+    const int g_lo = NF + std::min(NB, o * bchunk), g_hi = NF + std::min(NB, o * bchunk + bchunk);
+    const int nfo = f_hi - f_lo, n_own = nfo + (g_hi - g_lo);
+    for (int s0 = 0; s0 < n_own; s0 += 32) {
+      int w = 0;
+      for (int t = s0; t < std::min(n_own, s0 + 32); ++t) {
+        const int P = t < nfo ? f_lo + t : g_lo + (t - nfo);
+        const int j = gnode[no + P] - static_cast<int32_t>(no);
+        const int deg = rowptr[ro + j + 1] - rowptr[ro + j];
+        w = std::max(w, deg);
+        if (!ncode) continue;
+        const int64_t at = q + (t - s0);
+        nsell[no + P] = make_int2(static_cast<int>(at), deg);
+        for (int k = 0; k < deg; ++k) {
+          const int ic = inc[io + rowptr[ro + j] + k];
+          const int2 c = conn[fo + (ic >> 1)];
+          const int other = (ic & 1) ? c.x : c.y;
+          ncode[base + at + 32LL * k] = (code_of(pos[other]) << 1) | (ic & 1);
+          nfib[base + at + 32LL * k] = fo + (ic >> 1);
+        }
+      }
+      q += 32LL * w;
+    }
+  }
+  return q;
 }
 
 template <int CL, bool kAll>
@@ -1160,22 +1439,22 @@ cudaLaunchConfig_t launch_config(const MixedState& ms, unsigned grid, cudaStream
   return cfg;
 }
 
-template <int CL, bool kAll>
+template <int CL, bool kAll, bool kNodal>
 cudaError_t launch_bucket(const MixedState& ms, const DevBatch& b, const RunArgs& a, int q,
                           cudaStream_t s) {
   const int n = ms.bucket_off[q + 1] - ms.bucket_off[q];
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg =
       launch_config<CL, kAll>(ms, static_cast<unsigned>(ms.bucket_grid[q]), s, attr);
-  return cudaLaunchKernelEx(&cfg, relax_mixed_kernel<CL, kAll>, b, ms, a,
+  return cudaLaunchKernelEx(&cfg, relax_mixed_kernel<CL, kAll, kNodal>, b, ms, a,
                             static_cast<int>(ms.smem_bytes / sizeof(float)),
                             static_cast<const int32_t*>(ms.order + ms.bucket_off[q]), n,
                             ms.queues + q);
 }
 
-template <int CL, bool kAll>
+template <int CL, bool kAll, bool kNodal>
 cudaError_t setup_bucket(MixedState& ms, int n, int q) {
-  cudaError_t e = cudaFuncSetAttribute(relax_mixed_kernel<CL, kAll>,
+  cudaError_t e = cudaFuncSetAttribute(relax_mixed_kernel<CL, kAll, kNodal>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        ms.smem_bytes);
   if (e != cudaSuccess) return e;
@@ -1185,7 +1464,8 @@ cudaError_t setup_bucket(MixedState& ms, int n, int q) {
     cudaLaunchConfig_t cfg =
         launch_config<CL, kAll>(ms, static_cast<unsigned>(CL * ms.sms), nullptr, attr);
     clusters = 0;
-    if ((e = cudaOccupancyMaxActiveClusters(&clusters, relax_mixed_kernel<CL, kAll>, &cfg)) !=
+    if ((e = cudaOccupancyMaxActiveClusters(&clusters, relax_mixed_kernel<CL, kAll, kNodal>,
+                                            &cfg)) !=
         cudaSuccess)
       return e;
     if (clusters < 1) return cudaErrorInvalidConfiguration;
@@ -1199,7 +1479,7 @@ cudaError_t setup_bucket(MixedState& ms, int n, int q) {
 cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<RveDesc>& desc,
                          const std::vector<int2>& conn, const std::vector<int32_t>& rowptr,
                          const std::vector<int32_t>& inc, int sms, int max_cluster,
-                         cudaStream_t s) {
+                         bool serving_layout, cudaStream_t s) {
   cudaError_t e;
   const size_t nt = static_cast<size_t>(b.nt), et = static_cast<size_t>(b.et);
   if ((e = alloc(&ms.u_hl, 6 * nt)) != cudaSuccess) return e;
@@ -1241,10 +1521,15 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
   std::vector<int> rve_q(desc.size());
   ms.h_cl = new int32_t[std::max<size_t>(desc.size(), 1)];
   for (size_t r = 0; r < desc.size(); ++r) {
-    rve_q[r] = bucket_of(desc[r], smem_floats, max_cluster);
+    rve_q[r] = bucket_of(desc[r], smem_floats, max_cluster, serving_layout);
     bucket[rve_q[r]].push_back(static_cast<int32_t>(r));
     ms.h_cl[r] = kBucket[rve_q[r]].cl;
   }
+  if ((e = alloc(&ms.rve_bucket, desc.size())) != cudaSuccess ||
+      (!desc.empty() &&
+       (e = cudaMemcpy(ms.rve_bucket, rve_q.data(), desc.size() * sizeof(int32_t),
+                       cudaMemcpyHostToDevice)) != cudaSuccess))
+    return e;
   {
     // fiber order and codes of the cluster-solved RVEs
     std::vector<int2> econn(et);
@@ -1254,8 +1539,9 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
     for (int t = 0; t < nthr; ++t)
       pool.emplace_back([&, t] {
         for (size_t r = t; r < desc.size(); r += nthr)
-          cluster_order(desc[r], kBucket[rve_q[r]].cl, kBucket[rve_q[r]].all, smem_floats, conn,
-                        rowptr, inc, econn, icode, mslot, gnode, mrowptr);
+          cluster_order(desc[r], kBucket[rve_q[r]].cl,
+                        kBucket[rve_q[r]].all || kBucket[rve_q[r]].nodal, conn, rowptr, inc,
+                        econn, icode, mslot, gnode, mrowptr);
       });
     for (auto& th : pool) th.join();
     if ((e = cudaMemcpy(ms.econn, econn.data(), et * sizeof(int2), cudaMemcpyHostToDevice)) !=
@@ -1268,6 +1554,54 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
             cudaSuccess ||
         (e = cudaMemcpy(ms.mrowptr, mrowptr.data(), mrowptr.size() * sizeof(int32_t),
                         cudaMemcpyHostToDevice)) != cudaSuccess)
+      return e;
+
+    // SELL incidence blocks of the node-centric RVEs
+    std::vector<int64_t> sell_off(desc.size() + 1, 0);
+    {
+      std::vector<std::thread> sp;
+      for (int t = 0; t < nthr; ++t)
+        sp.emplace_back([&, t] {
+          for (size_t r = t; r < desc.size(); r += nthr)
+            if (kBucket[rve_q[r]].nodal)
+              sell_off[r + 1] = sell_layout(desc[r], kBucket[rve_q[r]].cl, conn, rowptr, inc,
+                                            gnode, 0, nullptr, nullptr, nullptr);
+        });
+      for (auto& th : sp) th.join();
+    }
+    for (size_t r = 0; r < desc.size(); ++r) sell_off[r + 1] += sell_off[r];
+    const int64_t n_sell = sell_off[desc.size()];
+    ms.n_sell = n_sell;
+    std::vector<int2> nsell(nt, make_int2(0, 0));
+    std::vector<int32_t> ncode(static_cast<size_t>(n_sell), 0);
+    std::vector<int64_t> nfib(static_cast<size_t>(n_sell), -1);
+    {
+      std::vector<std::thread> sp;
+      for (int t = 0; t < nthr; ++t)
+        sp.emplace_back([&, t] {
+          for (size_t r = t; r < desc.size(); r += nthr)
+            if (kBucket[rve_q[r]].nodal)
+              sell_layout(desc[r], kBucket[rve_q[r]].cl, conn, rowptr, inc, gnode, sell_off[r],
+                          nsell.data(), ncode.data(), nfib.data());
+        });
+      for (auto& th : sp) th.join();
+    }
+    if ((e = alloc(&ms.nsell, nt)) != cudaSuccess ||
+        (e = alloc(&ms.sell_off, desc.size())) != cudaSuccess ||
+        (e = alloc(&ms.ncode, static_cast<size_t>(n_sell))) != cudaSuccess ||
+        (e = alloc(&ms.nfc, static_cast<size_t>(n_sell))) != cudaSuccess ||
+        (e = alloc(&ms.nfib_tmp, static_cast<size_t>(n_sell))) != cudaSuccess)
+      return e;
+    if ((e = cudaMemcpy(ms.nsell, nsell.data(), nt * sizeof(int2), cudaMemcpyHostToDevice)) !=
+            cudaSuccess ||
+        (!desc.empty() &&
+         (e = cudaMemcpy(ms.sell_off, sell_off.data(), desc.size() * sizeof(int64_t),
+                         cudaMemcpyHostToDevice)) != cudaSuccess) ||
+        (n_sell > 0 &&
+         ((e = cudaMemcpy(ms.ncode, ncode.data(), n_sell * sizeof(int32_t),
+                          cudaMemcpyHostToDevice)) != cudaSuccess ||
+          (e = cudaMemcpy(ms.nfib_tmp, nfib.data(), n_sell * sizeof(int64_t),
+                          cudaMemcpyHostToDevice)) != cudaSuccess)))
       return e;
   }
   std::vector<int32_t> order;
@@ -1286,12 +1620,24 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
   for (int q = 0; q < kBuckets; ++q) {
     const int n = ms.bucket_off[q + 1] - ms.bucket_off[q];
     switch (q) {
-      case 0: e = setup_bucket<kBucket[0].cl, kBucket[0].all>(ms, n, q); break;
-      case 1: e = setup_bucket<kBucket[1].cl, kBucket[1].all>(ms, n, q); break;
-      case 2: e = setup_bucket<kBucket[2].cl, kBucket[2].all>(ms, n, q); break;
-      case 3: e = setup_bucket<kBucket[3].cl, kBucket[3].all>(ms, n, q); break;
-      case 4: e = setup_bucket<kBucket[4].cl, kBucket[4].all>(ms, n, q); break;
-      default: e = setup_bucket<kBucket[5].cl, kBucket[5].all>(ms, n, q); break;
+      case 0:
+        e = setup_bucket<kBucket[0].cl, kBucket[0].all, kBucket[0].nodal>(ms, n, q);
+        break;
+      case 1:
+        e = setup_bucket<kBucket[1].cl, kBucket[1].all, kBucket[1].nodal>(ms, n, q);
+        break;
+      case 2:
+        e = setup_bucket<kBucket[2].cl, kBucket[2].all, kBucket[2].nodal>(ms, n, q);
+        break;
+      case 3:
+        e = setup_bucket<kBucket[3].cl, kBucket[3].all, kBucket[3].nodal>(ms, n, q);
+        break;
+      case 4:
+        e = setup_bucket<kBucket[4].cl, kBucket[4].all, kBucket[4].nodal>(ms, n, q);
+        break;
+      default:
+        e = setup_bucket<kBucket[5].cl, kBucket[5].all, kBucket[5].nodal>(ms, n, q);
+        break;
     }
     if (e != cudaSuccess) return e;
     if ((e = cudaStreamCreateWithFlags(&ms.side[q], cudaStreamNonBlocking)) != cudaSuccess)
@@ -1312,7 +1658,17 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
   dim3 grid(static_cast<unsigned>((max_e + 255) / 256),
             static_cast<unsigned>(std::min(b.n_rve, 65535)));
   mixed_prepare_fibers_kernel<<<grid, 256, 0, s>>>(b, ms);
-  return cudaGetLastError();
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (ms.n_sell > 0) {
+    mixed_prepare_sell_kernel<<<static_cast<unsigned>((ms.n_sell + 255) / 256), 256, 0, s>>>(
+        ms, ms.nfib_tmp, ms.n_sell);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  // the fiber ids were only needed to fill the incidences' fiber data
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+  cudaFree(ms.nfib_tmp);
+  ms.nfib_tmp = nullptr;
+  return cudaSuccess;
 }
 
 int mixed_rve_cluster(const MixedState& ms, int rve) { return ms.h_cl ? ms.h_cl[rve] : 1; }
@@ -1352,12 +1708,24 @@ cudaError_t enqueue_buckets(MixedState& ms, const DevBatch& b, const RunArgs& a,
     cudaStream_t sq = ms.side[q];
     if ((e = cudaStreamWaitEvent(sq, ms.fork, 0)) != cudaSuccess) return e;
     switch (q) {
-      case 0: e = launch_bucket<kBucket[0].cl, kBucket[0].all>(ms, b, a, q, sq); break;
-      case 1: e = launch_bucket<kBucket[1].cl, kBucket[1].all>(ms, b, a, q, sq); break;
-      case 2: e = launch_bucket<kBucket[2].cl, kBucket[2].all>(ms, b, a, q, sq); break;
-      case 3: e = launch_bucket<kBucket[3].cl, kBucket[3].all>(ms, b, a, q, sq); break;
-      case 4: e = launch_bucket<kBucket[4].cl, kBucket[4].all>(ms, b, a, q, sq); break;
-      default: e = launch_bucket<kBucket[5].cl, kBucket[5].all>(ms, b, a, q, sq); break;
+      case 0:
+        e = launch_bucket<kBucket[0].cl, kBucket[0].all, kBucket[0].nodal>(ms, b, a, q, sq);
+        break;
+      case 1:
+        e = launch_bucket<kBucket[1].cl, kBucket[1].all, kBucket[1].nodal>(ms, b, a, q, sq);
+        break;
+      case 2:
+        e = launch_bucket<kBucket[2].cl, kBucket[2].all, kBucket[2].nodal>(ms, b, a, q, sq);
+        break;
+      case 3:
+        e = launch_bucket<kBucket[3].cl, kBucket[3].all, kBucket[3].nodal>(ms, b, a, q, sq);
+        break;
+      case 4:
+        e = launch_bucket<kBucket[4].cl, kBucket[4].all, kBucket[4].nodal>(ms, b, a, q, sq);
+        break;
+      default:
+        e = launch_bucket<kBucket[5].cl, kBucket[5].all, kBucket[5].nodal>(ms, b, a, q, sq);
+        break;
     }
     if (e != cudaSuccess) return e;
     ++*launches;

@@ -92,11 +92,11 @@ def test_mixed_incremental_and_transactional_runs(M):
 
 
 def test_mixed_every_placement_and_cluster_size(M):
-    """One RVE per way a batch run places an RVE: all mutable state in one
-    CTA's shared memory (800 nodes), all of it split over clusters of 2 and 4
-    CTAs (4,000 / 9,000 nodes), node state only over clusters of 4 and 8
-    (20,000 / 40,000) and global memory (80,000). Each agrees with FP64, and
-    each gives the same bits solved alone as in the mixed-size batch."""
+    """One RVE per way a batch run places an RVE: fiber-centric with all
+    mutable state in one CTA's shared memory (800 nodes), node-centric on one
+    CTA (4,000) and over clusters of 2, 4 and 8 CTAs (9,000 / 20,000 /
+    40,000), fiber-centric in global memory (80,000). Each agrees with FP64,
+    and each gives the same bits solved alone as in the mixed-size batch."""
     from mumfim_gb300 import synthetic as S
     sizes = (800, 4_000, 9_000, 20_000, 40_000, 80_000)
     nets, F = [], []
@@ -120,12 +120,13 @@ def test_mixed_every_placement_and_cluster_size(M):
 
 
 def test_cluster_and_single_cta_solves_agree(M):
-    """The same RVEs solved over thread-block clusters (2, 4 and 8 CTAs, with
-    all state or node state only on chip) and on one CTA each
-    (max_cluster_ctas=1): the same per-fiber and per-node arithmetic in the
-    same order, so the same bits, in RAMP mode and in RELAX mode (there the
-    step count too; only the residual's last bits may differ, since the
-    cluster sums it in per-CTA parts)."""
+    """The same RVEs solved node-centric over thread-block clusters (1, 2, 4
+    and 8 CTAs), in the serving layout (clusters of 4 instead of 2) and on
+    one CTA each (max_cluster_ctas=1: node-centric where the node state
+    fits, else fiber-centric with run-time placement): the same per-fiber
+    and per-node arithmetic in the same order, so the same bits, in RAMP
+    mode and in RELAX mode (there the step count too; only the residual's
+    last bits may differ, since a cluster sums it in per-CTA parts)."""
     from mumfim_gb300 import synthetic as S
     sizes = (4_000, 9_000, 20_000, 40_000)
     nets, F = [], []
@@ -137,19 +138,20 @@ def test_cluster_and_single_cta_solves_agree(M):
     for strat in (M.SolutionStrategy.ramp(800, 0.5),
                   M.SolutionStrategy(visc_damp_coeff=0.5, residual_tol=1e-6, max_steps=1_500)):
         out = []
-        for mc in (0, 1):
+        for mc, sl in ((0, False), (1, False), (0, True)):
             g = M.BatchedFiberRVEAnalysisExplicit(nets, [strat] * len(nets), precision="mixed",
-                                                  max_cluster_ctas=mc)
+                                                  max_cluster_ctas=mc, serving_layout=sl)
             s = np.zeros((len(nets), 6))
             g.run(F, s)
             out.append((s, g.last_status.copy(), g.displacements(2)))
             g.close()
-        (s0, st0, u0), (s1, st1, u1) = out
-        np.testing.assert_array_equal(s0, s1)
-        np.testing.assert_array_equal(u0, u1)
-        np.testing.assert_array_equal(st0["steps"], st1["steps"])
-        np.testing.assert_array_equal(st0["status"], st1["status"])
-        np.testing.assert_allclose(st0["residual"], st1["residual"], rtol=1e-9)
+        s0, st0, u0 = out[0]
+        for s1, st1, u1 in out[1:]:
+            np.testing.assert_array_equal(s0, s1)
+            np.testing.assert_array_equal(u0, u1)
+            np.testing.assert_array_equal(st0["steps"], st1["steps"])
+            np.testing.assert_array_equal(st0["status"], st1["status"])
+            np.testing.assert_allclose(st0["residual"], st1["residual"], rtol=1e-9)
 
 
 def test_max_cluster_ctas_is_checked(M):

@@ -105,11 +105,12 @@ def test_admission_ring_full_and_idle_relaunch(W):
 
 
 def test_server_placements_match_clustered_batch(lib_path):
-    """The serving kernel solves every RVE on one CTA (all state in shared
-    memory at 1,000 nodes, node state at 5,000, displacements only at 8,000,
-    global memory at 12,000) while a batch run splits the larger ones over
-    clusters of 2 to 8 CTAs: the ramped stress is the same bits either way
-    (same per-fiber and per-node arithmetic, and dt is a minimum)."""
+    """The serving kernel solves each RVE with the solve of its bucket in the
+    serving layout: fiber-centric on one CTA (1,000 nodes), node-centric on
+    one CTA (5,000) and node-centric over clusters of 4 (8,000 and 12,000),
+    while a batch run takes a cluster of 2 for 8,000: the ramped stress is
+    the same bits either way (same per-fiber and per-node arithmetic, and dt
+    is a minimum)."""
     import mumfim_gb300 as m
     from mumfim_gb300 import synthetic as S
     from mumfim_gb300.serving import RVEServer
