@@ -841,6 +841,50 @@ __device__ __forceinline__ void nodal_force(const Law& L, const Nodes& u, const 
   }
 }
 
+// Pass A of the node-centric step: force and kick (v += hk f / m - damping)
+// of the CTA's own free nodes t = tid, tid + kThreadsMixed, ... < nfo, the
+// next node's row and mass loaded while the current one is summed. With
+// kRes also returns this thread's share of the squared residual norm.
+template <bool kRes, class Nodes>
+__device__ __forceinline__ double nodal_kick(const Law& L, const Nodes& u, const LocalNodes& own,
+                                             float* vel, const int32_t* ncode, const float4* nfc,
+                                             const int2* srow, const float2* mass, int nfo,
+                                             float hk, float c) {
+  double part = 0.0;
+  int t = threadIdx.x;
+  if (t >= nfo) return part;
+  int2 sr = __ldg(srow + t);
+  float2 mm = __ldg(mass + t);
+  for (;;) {
+    const int tn = t + kThreadsMixed;
+    const bool more = tn < nfo;
+    int2 srn = sr;
+    float2 mmn = mm;
+    if (more) {
+      srn = __ldg(srow + tn);
+      mmn = __ldg(mass + tn);
+    }
+    float f[3];
+    nodal_force(L, u, ncode, nfc, sr.x, sr.y, own.load(t), f[0], f[1], f[2]);
+    if constexpr (kRes)
+      part += static_cast<double>(f[0]) * f[0] + static_cast<double>(f[1]) * f[1] +
+              static_cast<double>(f[2]) * f[2];
+    const float mc = mm.y * c;
+    const float km = hk * mm.x;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float w = vel[3 * t + k];
+      w = fmaf(km, -f[k] - mc * w, w);
+      vel[3 * t + k] = w;
+    }
+    if (!more) break;
+    t = tn;
+    sr = srn;
+    mm = mmn;
+  }
+  return part;
+}
+
 // Shortest current length among fiber slots e_lo + tid, + kThreadsMixed, ...
 // < e_hi (the critical time step's input, every 100 steps).
 template <class Nodes>
@@ -936,41 +980,12 @@ __device__ void solve_rve_nodal(const DevBatch& b, const MixedState& ms, const R
     }
     const float h = h_cur;
     const float hk = h_prev + h;  // trailing kick of step-1 + leading kick of step
-    // pass A: force and kick of the own free nodes, the next node's row and
-    // mass loaded while the current one is summed
-    double part = 0.0;
-    if (tid < nfo) {
-      int t = tid;
-      int2 sr = __ldg(srow + f_lo + t);
-      float2 mm = __ldg(mass + f_lo + t);
-      for (;;) {
-        const int tn = t + kThreadsMixed;
-        const bool more = tn < nfo;
-        int2 srn = sr;
-        float2 mmn = mm;
-        if (more) {
-          srn = __ldg(srow + f_lo + tn);
-          mmn = __ldg(mass + f_lo + tn);
-        }
-        float f[3];
-        nodal_force(r.L, u, ncode, nfc, sr.x, sr.y, own.load(t), f[0], f[1], f[2]);
-        if (res_step)
-          part += static_cast<double>(f[0]) * f[0] + static_cast<double>(f[1]) * f[1] +
-                  static_cast<double>(f[2]) * f[2];
-        const float mc = mm.y * c;
-        const float km = hk * mm.x;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          float w = vel[3 * t + k];
-          w = fmaf(km, -f[k] - mc * w, w);
-          vel[3 * t + k] = w;
-        }
-        if (!more) break;
-        t = tn;
-        sr = srn;
-        mm = mmn;
-      }
-    }
+    // pass A (compiled apart for the residual steps, so that the FP64
+    // residual sum costs nothing on the others)
+    const double part =
+        res_step ? nodal_kick<true>(r.L, u, own, vel, ncode, nfc, srow + f_lo, mass + f_lo, nfo, hk, c)
+                 : nodal_kick<false>(r.L, u, own, vel, ncode, nfc, srow + f_lo, mass + f_lo, nfo, hk,
+                                     c);
     if (res_step) {
       residual = sqrt(Ops::template combine<false>(block_sum<kThreadsMixed>(part, red), cred));
       if (!isfinite(residual)) {
@@ -1280,17 +1295,21 @@ int bucket_of(const RveDesc& d, int smem_floats, int max_cluster, bool serving_l
 // shared memory.
 //
 // Nodes: within each CTA's block of free nodes, those whose neighbours are
-// all owned by that CTA come first, and within each group the nodes of fewer
-// incident fibers, so the lanes of a warp run loops of nearly the same
-// length (+6 % for the fiber-centric single CTA) and the warps that wait on
-// other CTAs are few. Boundary nodes keep their places.
+// all owned by that CTA come first, and within each group the nodes by
+// degree, so the lanes of a warp run loops of nearly the same length (+6 %
+// for the fiber-centric single CTA) and the warps that wait on other CTAs
+// are few. heavy_first (node-centric solve) orders by falling degree, so the
+// threads' last, partial round over the nodes gets the lightest ones (+13 %
+// on config 2 against rising degree); the fiber-centric solve keeps rising
+// degree. Boundary nodes keep their places.
 //
 // Writes the fiber positions (mslot), the end-node codes by position
 // (econn), the node index by node position (gnode, batch-wide), and the CSR
 // rows by node position (mrowptr) with their incidences as (fiber position
 // << 1 | end) (icode), which the single-CTA fiber-centric solve reads. RVEs
 // without their own order (own_order false) keep the batch's order.
-void cluster_order(const RveDesc& d, int cl, bool own_order, const std::vector<int2>& conn,
+void cluster_order(const RveDesc& d, int cl, bool own_order, bool heavy_first,
+                   const std::vector<int2>& conn,
                    const std::vector<int32_t>& rowptr, const std::vector<int32_t>& inc,
                    std::vector<int2>& econn, std::vector<int32_t>& icode,
                    std::vector<int32_t>& mslot, std::vector<int32_t>& gnode,
@@ -1324,7 +1343,7 @@ void cluster_order(const RveDesc& d, int cl, bool own_order, const std::vector<i
   for (int j = 0; j < N; ++j) pos[j] = j;
   for (int o = 0; o < cl; ++o) {
     const int f_lo = std::min(NF, o * fchunk), f_hi = std::min(NF, f_lo + fchunk);
-    std::vector<std::pair<int, int>> order;  // (group * 1024 + degree, node)
+    std::vector<std::pair<int, int>> order;  // (group * 1024 + degree rank, node)
     order.reserve(f_hi - f_lo);
     for (int j = f_lo; j < f_hi; ++j) {
       bool local = true;
@@ -1334,7 +1353,7 @@ void cluster_order(const RveDesc& d, int cl, bool own_order, const std::vector<i
         local = owner((ic & 1) ? c.x : c.y) == o;
       }
       const int deg = std::min(rowptr[ro + j + 1] - rowptr[ro + j], 1023);
-      order.emplace_back((local ? 0 : 1024) + deg, j);
+      order.emplace_back((local ? 0 : 1024) + (heavy_first ? 1023 - deg : deg), j);
     }
     std::stable_sort(order.begin(), order.end(),
                      [](const std::pair<int, int>& x, const std::pair<int, int>& y) {
@@ -1540,8 +1559,9 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
       pool.emplace_back([&, t] {
         for (size_t r = t; r < desc.size(); r += nthr)
           cluster_order(desc[r], kBucket[rve_q[r]].cl,
-                        kBucket[rve_q[r]].all || kBucket[rve_q[r]].nodal, conn, rowptr, inc,
-                        econn, icode, mslot, gnode, mrowptr);
+                        kBucket[rve_q[r]].all || kBucket[rve_q[r]].nodal,
+                        kBucket[rve_q[r]].nodal, conn, rowptr, inc, econn, icode, mslot, gnode,
+                        mrowptr);
       });
     for (auto& th : pool) th.join();
     if ((e = cudaMemcpy(ms.econn, econn.data(), et * sizeof(int2), cudaMemcpyHostToDevice)) !=
