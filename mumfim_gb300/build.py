@@ -32,6 +32,7 @@ SOURCES = [
     ("mfg_host.cpp", "cxx", []),
     ("netgen.cpp", "cxx", []),
     ("mfg_coupling.cpp", "cxx", []),
+    ("mfg_mixed_order.cpp", "cxx", []),
     ("mfg_relax_f64.cu", "cuda", ["--fmad=false"]),
     ("mfg_aux.cu", "cuda", ["--fmad=false"]),
     ("mfg_relax_mixed.cu", "cuda", []),
