@@ -23,15 +23,21 @@
 //    of the batch (x, u, volume), read at the start and written at the end
 //    of every run, so both precisions share it.
 //
+// Two solves give the same bits: a fiber-centric one (a fiber pass stores
+// each fiber's force vector, a node pass gathers them) and a node-centric
+// one (each node forms its incident fibers' vectors from the end records;
+// nothing but the node state in shared memory).
+//
 // Placement: one CTA of 1024 threads per SM with 220 KB of dynamic shared
-// memory. An RVE is solved by one CTA or by the 2, 4 or 8 CTAs of a
-// thread-block cluster, in size buckets launched concurrently; each CTA
-// keeps its nodes' records (hi, lo) and velocities and, where they fit, its
-// fibers' force vectors in shared memory, reading other CTAs' through
-// distributed shared memory. Cluster-solved and all-on-chip RVEs get their
-// own fiber and node order (cluster_order) that keeps most loads local and
-// the warps' work even. The largest RVEs and the serving kernels' single-CTA
-// solves place by size at run time, down to global memory.
+// memory, in size buckets launched concurrently. RVEs whose whole state fits
+// one CTA's shared memory run fiber-centric on one CTA; larger ones run
+// node-centric on one CTA or on the 2, 4 or 8 CTAs of a thread-block
+// cluster, each CTA keeping its nodes' records (hi, lo) and velocities in
+// shared memory and reading other CTAs' through distributed shared memory.
+// Those RVEs get their own fiber and node order (cluster_order) that keeps
+// most loads local and the warps' work even. RVEs too large for a cluster of
+// 8 run fiber-centric on one CTA, placed by size at run time down to global
+// memory.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -51,26 +57,23 @@ namespace cg = cooperative_groups;
 namespace mfg {
 
 struct MixedState {
-  float* u_hl = nullptr;   // 6 * nt, node records (hi x, y, z, lo x, y, z); STREAM placement
-  float* v = nullptr;      // 3 * nt, velocity (x, y, z per node); placements without it on chip
+  float* u_hl = nullptr;   // 6 * nt, node records (hi x, y, z, lo x, y, z); run-time placement
+  float* v = nullptr;      // 3 * nt, velocity (x, y, z per node); run-time placement
   float2* mass = nullptr;  // nt, (1 / m, m)
   float4* fcon = nullptr;  // et, (X[n2] - X[n1], 1 / l0) rounded to FP32
-  float4* nrm = nullptr;   // et, per-fiber force vectors (scratch; w unused)
-  // Cluster-solved and all-on-chip RVEs have their own fiber order (see
-  // cluster_order): per fiber position the two end nodes as (owner CTA << 24
-  // | local record) and the read-only data, per CSR incidence the force
-  // vector as (flag | owner CTA << 24 | local position << 1 | end) when it is
-  // in a CTA's shared memory, else (position << 1 | end). The runtime-
-  // placement solve (largest RVEs, serving kernels' single-CTA requests)
-  // uses the batch's own order, node ids and incidence codes.
+  float4* nrm = nullptr;   // et, per-fiber force vectors of the run-time placement (w unused)
+  // RVEs with an order of their own (cluster_order: all but the run-time
+  // placement): per fiber position the two end nodes as (owner CTA << 24 |
+  // local record) and the read-only data, per CSR incidence (fiber position
+  // << 1 | end). The run-time placement uses the batch's own order, node ids
+  // and incidence codes.
   int2* econn = nullptr;      // et
   float4* fconc = nullptr;    // et
   int32_t* icode = nullptr;   // 2 * et
   int32_t* mslot = nullptr;   // et, position of each fiber slot in that order
-  // Their nodes: each CTA's free nodes whose force vectors are all in its
-  // shared memory come first, ordered by degree in the all-on-chip buckets;
-  // gnode maps a node position to the batch node index, and the CSR rows and
-  // masses follow the positions.
+  // Their nodes: each CTA's free nodes whose neighbours are all its own come
+  // first, each group ordered by degree; gnode maps a node position to the
+  // batch node index, and the CSR rows and masses follow the positions.
   int32_t* gnode = nullptr;    // nt
   int32_t* mrowptr = nullptr;  // nt + n_rve
   float2* mmass = nullptr;     // nt
@@ -88,9 +91,9 @@ struct MixedState {
   int server_grid = 0;         // CTAs of the cluster serving kernel
   int sms = 1;
   int smem_bytes = 0;
-  // Size buckets of the batch run (kBucket[q]: cluster size, force vectors
-  // in shared memory); the RVEs of bucket q, most fibers first, are
-  // order[bucket_off[q] .. bucket_off[q + 1]).
+  // Size buckets of the batch run (kBucket[q]: cluster size and solve); the
+  // RVEs of bucket q, most fibers first, are order[bucket_off[q] ..
+  // bucket_off[q + 1]).
   int32_t* order = nullptr;
   int32_t* queues = nullptr;  // one claim counter per bucket
   int bucket_off[7] = {};
@@ -319,7 +322,7 @@ struct ClusterOps {
     return 0;
   }
   // Block barrier, or cluster barrier (release / acquire at cluster scope,
-  // which also orders global-memory force vectors between CTAs).
+  // which also orders the CTAs' shared-memory writes for their peers).
   __device__ static void sync() {
     if constexpr (CL > 1)
       cg::this_cluster().sync();
@@ -514,10 +517,10 @@ __device__ __forceinline__ void mixed_stress(const DevBatch& b, const RunArgs& a
   }
 }
 
-// Shared-memory floats of an RVE solved by a cluster of CL CTAs: 9 per node
-// slot of a CTA (displacement hi, lo and velocity; ceil(NF/CL) free plus
-// ceil(NB/CL) boundary slots), plus 4 per fiber slot (ceil(E/CL)) when the
-// force vectors are kept in shared memory too (all).
+// Shared-memory floats per CTA of an RVE solved by CL CTAs: 9 per node slot
+// (displacement hi, lo and velocity; ceil(NF/CL) free plus ceil(NB/CL)
+// boundary slots), plus 4 per fiber slot (ceil(E/CL)) when the force vectors
+// are kept in shared memory too (all: the fiber-centric single CTA).
 __host__ __device__ inline int64_t cluster_floats(int n_nodes, int n_free, int n_fibers, int cl,
                                                   bool all) {
   const int64_t nb = n_nodes - n_free;
