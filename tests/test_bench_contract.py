@@ -1,0 +1,49 @@
+"""The benchmark's command-line contract, checked on the CPU.
+
+`bench.py --impl reference` times the reference's CPU path (the oracle port)
+and prints one JSON line with the keys every arm prints; the GPU arm must
+fail loudly, not fall back, when there is no GPU."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _run(args, timeout=300):
+    return subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), *args], cwd=ROOT,
+                          capture_output=True, text=True, timeout=timeout)
+
+
+def test_reference_arm_prints_one_contract_line():
+    r = _run(["--impl", "reference", "--steps", "1", "--warmup", "3", "--n-rve", "8",
+              "--cpu-sample-rves", "2", "--solve-steps", "100"])
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference"
+    assert d["metric"] == "fiber-steps/s" and d["unit"] == "fiber-steps/s"
+    assert d["value"] > 0 and d["higher_is_better"] is True
+    assert d["n_gpus"] == 1 and d["steps"] == 1 and d["warmup"] == 3
+    assert d["scaling"] == "weak" and d["vs_baseline"] is None
+    assert d["ms_per_step"] > 0 and "workload" in d["config"]
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert cb["unit"] == d["unit"] and cb["sample"]
+    e2e = d["e2e"]
+    assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
+    assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_gpu_arm_fails_without_a_gpu():
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    r = _run(["--n-rve", "4", "--solve-steps", "10", "--steps", "1", "--warmup", "3",
+              "--no-extras", "--no-cpu-baseline"], timeout=120)
+    assert r.returncode != 0
+    assert not [x for x in r.stdout.splitlines() if x.startswith("{")]
