@@ -96,3 +96,24 @@ def test_valid_input_without_gpu_reports_no_device(lib_path):
     with pytest.raises(m.MumfimGpuError) as ei:
         m.BatchedFiberRVEAnalysisExplicit([_net()], [m.SolutionStrategy()])
     assert ei.value.status == 7
+
+
+@pytest.mark.parametrize("field,value,msg", [
+    ("max_cluster_ctas", 3, "max_cluster_ctas"), ("cluster_layout", 7, "cluster_layout"),
+    ("precision", 5, "precision"),
+])
+def test_bad_options_are_rejected_before_the_device(lib_path, field, value, msg):
+    """Option checks come before any device call, so they hold on a machine
+    without a GPU too."""
+    from mumfim_gb300 import SolutionStrategy, _abi
+    from mumfim_gb300.batched import load_library
+    L = load_library()
+    arr = _abi.NetworkArray([_net()], [SolutionStrategy()])
+    o = _abi.mfg_options()
+    L.mfg_default_options(C.byref(o))
+    o.precision = 1
+    setattr(o, field, value)
+    h = C.c_void_p()
+    assert L.mfg_batch_create(arr.nets, arr.strats, 1, C.byref(o), C.byref(h)) == 1
+    assert msg in L.mfg_last_error().decode()
+    assert not h.value
