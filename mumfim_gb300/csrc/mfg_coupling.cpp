@@ -6,6 +6,7 @@
 #include <cstring>
 #include <vector>
 
+#include "mfg_internal.h"
 #include "mumfim_gpu.h"
 
 namespace mfg {
@@ -48,6 +49,7 @@ mfg_status mfg_scale_conversion(int32_t n_nodes, const double* coords, int32_t n
 
 mfg_status mfg_batch_micro_fo_iterate(mfg_batch* batch, const double* data, double* results,
                                       mfg_rve_status* status) {
+  mfg::Trace trace("mfg_batch_micro_fo_iterate");
   if (!batch || !data || !results) return set_error(MFG_E_INVALID, "NULL argument");
   const int32_t R = mfg_batch_size(batch);
   if (R < 1) return set_error(MFG_E_INVALID, "empty batch");
@@ -67,6 +69,7 @@ mfg_status mfg_batch_micro_fo_iterate(mfg_batch* batch, const double* data, doub
 }
 
 mfg_status mfg_batch_micro_fo_step(mfg_batch* batch, const double* params, double* step_results) {
+  mfg::Trace trace("mfg_batch_micro_fo_step");
   if (!batch || !params || !step_results) return set_error(MFG_E_INVALID, "NULL argument");
   const int32_t R = mfg_batch_size(batch);
   if (R < 1) return set_error(MFG_E_INVALID, "empty batch");

@@ -413,6 +413,7 @@ void mfg_default_options(mfg_options* out) {
 
 mfg_status mfg_batch_create(const mfg_network* nets, const mfg_strategy* strategies,
                             int32_t n_rve, const mfg_options* options, mfg_batch** out) {
+  mfg::Trace trace("mfg_batch_create");
   g_last_error.clear();
   if (!out) return fail(MFG_E_INVALID, "out is NULL");
   *out = nullptr;
@@ -626,6 +627,7 @@ int32_t mfg_batch_n_fibers(const mfg_batch* b, int32_t r) {
 
 mfg_status mfg_batch_run_device(mfg_batch* b, const double* F_dev, int32_t n_F, double* sigma_dev,
                                 int32_t update_coords, mfg_rve_status* status_dev, void* stream) {
+  mfg::Trace trace("mfg_batch_run_device");
   g_last_error.clear();
   if (!b || !F_dev || !sigma_dev) return fail(MFG_E_INVALID, "NULL argument");
   mfg_status st = check_run_args(b, n_F, update_coords);
@@ -649,6 +651,7 @@ mfg_status mfg_batch_run_device(mfg_batch* b, const double* F_dev, int32_t n_F, 
 mfg_status mfg_batch_run_device_noalloc(mfg_batch* b, const double* F_dev, int32_t n_F,
                                         double* sigma_dev, int32_t update_coords,
                                         mfg_rve_status* status_dev, void* stream) {
+  mfg::Trace trace("mfg_batch_run_device_noalloc");
   g_last_error.clear();
   if (!b || !F_dev || !sigma_dev) return fail(MFG_E_INVALID, "NULL argument");
   if (b->precision != MFG_PREC_F64)
@@ -688,6 +691,7 @@ mfg_status mfg_batch_run_device_noalloc(mfg_batch* b, const double* F_dev, int32
 
 mfg_status mfg_batch_run(mfg_batch* b, const double* F, int32_t n_F, double* sigma,
                          int32_t update_coords, mfg_rve_status* status) {
+  mfg::Trace trace("mfg_batch_run");
   g_last_error.clear();
   if (!b || !F || !sigma) return fail(MFG_E_INVALID, "NULL argument");
   mfg_status st = check_run_args(b, n_F, update_coords);
@@ -721,6 +725,7 @@ mfg_status mfg_batch_run(mfg_batch* b, const double* F, int32_t n_F, double* sig
 }
 
 mfg_status mfg_batch_material_stiffness(mfg_batch* b, double* C) {
+  mfg::Trace trace("mfg_batch_material_stiffness");
   g_last_error.clear();
   if (!b || !C) return fail(MFG_E_INVALID, "NULL argument");
   MFG_CUDA(cudaSetDevice(b->device));
@@ -759,6 +764,7 @@ mfg_status mfg_batch_orientation_3d(mfg_batch* b, double* omega) {
 }
 
 mfg_status mfg_batch_orientation_2d(mfg_batch* b, const double* normal, double* omega) {
+  mfg::Trace trace("mfg_batch_orientation");
   g_last_error.clear();
   if (!b || !omega) return fail(MFG_E_INVALID, "NULL argument");
   MFG_CUDA(cudaSetDevice(b->device));
@@ -815,6 +821,7 @@ size_t mfg_batch_state_bytes(const mfg_batch* b, int32_t rve) {
 }
 
 mfg_status mfg_batch_export_state(mfg_batch* b, int32_t rve, void* buf, size_t bytes) {
+  mfg::Trace trace("mfg_batch_export_state");
   g_last_error.clear();
   if (!b || !buf || rve < 0 || rve >= b->R) return fail(MFG_E_INVALID, "bad rve or NULL buffer");
   if (bytes < mfg_batch_state_bytes(b, rve)) return fail(MFG_E_INVALID, "buffer too small");
@@ -836,6 +843,7 @@ mfg_status mfg_batch_export_state(mfg_batch* b, int32_t rve, void* buf, size_t b
 }
 
 mfg_status mfg_batch_import_state(mfg_batch* b, int32_t rve, const void* buf, size_t bytes) {
+  mfg::Trace trace("mfg_batch_import_state");
   g_last_error.clear();
   if (!b || !buf || rve < 0 || rve >= b->R) return fail(MFG_E_INVALID, "bad rve or NULL buffer");
   if (bytes < mfg_batch_state_bytes(b, rve)) return fail(MFG_E_INVALID, "buffer too small");
@@ -1081,6 +1089,7 @@ void mfg_default_server_options(mfg_server_options* out) {
 
 mfg_status mfg_server_create(const mfg_network* nets, const mfg_strategy* strategies,
                              int32_t n_rve, const mfg_server_options* options, mfg_server** out) {
+  mfg::Trace trace("mfg_server_create");
   g_last_error.clear();
   if (!out) return fail(MFG_E_INVALID, "out is NULL");
   *out = nullptr;
@@ -1243,6 +1252,7 @@ int64_t mfg_server_launches(const mfg_server* sv) { return sv ? sv->launches : 0
 mfg_batch* mfg_server_batch(mfg_server* sv) { return sv ? sv->batch : nullptr; }
 
 mfg_status mfg_server_destroy(mfg_server* sv) {
+  mfg::Trace trace("mfg_server_destroy");
   delete sv;
   return MFG_OK;
 }

@@ -15,8 +15,20 @@
 #include <cstdint>
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 namespace mfg {
+
+// A named NVTX range for the duration of a scope: the phases of each call
+// as a profiler shows them (Nsight Systems, ncu --nvtx), the counterpart of
+// the reference's Kokkos kernel labels for Kokkos Tools. Without a tool
+// attached a push or pop is a branch.
+struct Trace {
+  explicit Trace(const char* name) { nvtxRangePushA(name); }
+  ~Trace() { nvtxRangePop(); }
+  Trace(const Trace&) = delete;
+  Trace& operator=(const Trace&) = delete;
+};
 
 constexpr int kUpdateFreq = 100;  // dt and residual refresh period (TeamOuterLoop.h:4)
 
