@@ -47,3 +47,23 @@ def test_gpu_arm_fails_without_a_gpu():
               "--no-extras", "--no-cpu-baseline"], timeout=120)
     assert r.returncode != 0
     assert not [x for x in r.stdout.splitlines() if x.startswith("{")]
+
+
+def test_reference_arm_under_torchrun_prints_once():
+    """With N ranks, rank 0 alone runs the reference arm and prints; the
+    others exit 0 without work."""
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+                        "--nproc-per-node", "2", "--master-addr", "127.0.0.1", "--master-port",
+                        str(port), os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                        "--gpus", "2", "--steps", "1", "--warmup", "3", "--n-rve", "8",
+                        "--cpu-sample-rves", "2", "--solve-steps", "100"],
+                       cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
