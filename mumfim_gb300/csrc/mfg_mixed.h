@@ -14,9 +14,12 @@ namespace mfg {
 struct MixedState;
 MixedState* mixed_new();
 
-// Allocates the mixed-precision working set of a batch.
-// conn, rowptr and inc are the batch's packed fiber ends and CSR rows on the
-// host (the cluster-solved RVEs get their own fiber and node order from them).
+// Allocates the mixed-precision working set of a batch and places its RVEs
+// in size buckets. conn, rowptr and inc are the batch's packed fiber ends
+// and CSR rows on the host (RVEs with an order of their own, and the
+// node-centric incidence blocks, are built from them). max_cluster bounds
+// the cluster size; serving_layout takes clusters of 4 where the batch
+// layout would take 2.
 cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<RveDesc>& desc,
                          const std::vector<int2>& conn, const std::vector<int32_t>& rowptr,
                          const std::vector<int32_t>& inc, int sms, int max_cluster,
