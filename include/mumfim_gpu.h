@@ -255,8 +255,10 @@ mfg_status mfg_batch_micro_fo_step(mfg_batch* batch, const double* params, doubl
 
 /* ---- solve without allocating ------------------------------------------ */
 /* Size of the device array that mfg_batch_run_device_noalloc() takes its
- * scratch from (16 MiB). Every GPU that loads this library holds it until the
- * process exits. */
+ * scratch from (16 MiB). mfg_batch_create() of an FP64 batch reserves it on
+ * the batch's device (CUDA loads the code that holds it lazily, and the
+ * create call forces that load), and the device holds it until the process
+ * exits. */
 #define MFG_NOALLOC_SCRATCH_BYTES (16u << 20)
 
 /* No counterpart in the reference. Same solve as mfg_batch_run_device() on
@@ -273,9 +275,10 @@ mfg_status mfg_batch_micro_fo_step(mfg_batch* batch, const double* params, doubl
  *  - Scratch need: 8 * (3 * fibers + 3 * nodes + 6 * boundary nodes) bytes
  *    over the whole batch plus 16 bytes per RVE (each piece rounded up to 256
  *    bytes). Larger batches get MFG_E_INVALID with the need in the message.
- *  - The first call on a device looks up the array's device address (once
- *    per device, with that device current); make that first call before any
- *    stream capture.
+ *  - Every call looks up the array's device address with the batch's device
+ *    current (a lookup, no allocation: the batch's creation already loaded
+ *    the array). Do not use a batch across a cudaDeviceReset() of its
+ *    device: the reset frees the batch's memory and the array with it.
  *  - Every call shares the one array: calls whose work overlaps on the GPU
  *    (other streams, other batches, other host threads) race on it and must
  *    be serialised by the caller. The array keeps the last call's contents;
@@ -307,7 +310,10 @@ typedef struct mfg_server_options {
   int32_t capacity;         /* request ring entries; 0 = 65536 */
   int32_t idle_timeout_us;  /* persistent kernel exits after this long without work; 0 = 20000 */
   double hbm_budget_bytes;  /* admission cap on the device state of all RVEs; 0 = free HBM */
-  int32_t reserved[4];
+  int32_t max_wait_ms;      /* longest a persistent-kernel CTA waits for work before it
+                               leaves (device time; a host that stalls or is abandoned
+                               frees the SMs within this); 0 = 5000 */
+  int32_t reserved[3];
 } mfg_server_options;
 
 /* One completed request. sigma maps onto micro_fo_result.data[0..5]

@@ -6,9 +6,12 @@ increment in, homogenised Cauchy stress and updated RVE state out. The
 compute path is libmumfim_gpu.so (hand-written sm_103a CUDA behind the C ABI
 of include/mumfim_gpu.h); this package only binds it.
 """
-from .batched import BatchedFiberRVEAnalysisExplicit, MumfimGpuError, load_library
+from ._abi import RVE_STATUS_DTYPE
+from .batched import (NOALLOC_SCRATCH_BYTES, BatchedFiberRVEAnalysisExplicit, MumfimGpuError,
+                      load_library)
 from .network_io import FiberNetwork, Reaction, load_network
 from .strategy import SolutionStrategy
 
 __all__ = ["BatchedFiberRVEAnalysisExplicit", "MumfimGpuError", "load_library", "FiberNetwork",
-           "Reaction", "load_network", "SolutionStrategy"]
+           "Reaction", "load_network", "SolutionStrategy", "RVE_STATUS_DTYPE",
+           "NOALLOC_SCRATCH_BYTES"]

@@ -98,7 +98,7 @@ class NetworkArray:
 class mfg_server_options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("device", C.c_int32), ("capacity", C.c_int32),
                 ("idle_timeout_us", C.c_int32), ("hbm_budget_bytes", C.c_double),
-                ("reserved", C.c_int32 * 4)]
+                ("max_wait_ms", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 SERVER_RESULT_DTYPE = np.dtype([("ticket", np.int64), ("rve", np.int32), ("status", np.int32),

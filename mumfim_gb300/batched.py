@@ -28,6 +28,9 @@ from ._abi import (MFG_E_NOT_CONVERGED, MFG_E_NONFINITE, MFG_OK, MFG_PREC_F64, M
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_PKG, "_lib", "libmumfim_gpu.so")
+# MFG_NOALLOC_SCRATCH_BYTES: size of the fixed device array the no-allocation
+# solve takes its scratch from
+NOALLOC_SCRATCH_BYTES = 16 << 20
 
 _lib = None
 

@@ -123,11 +123,21 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // may start closing only when every CTA of the grid is waiting and no
 // request has been claimed anywhere for `idle_ns`; closing sets a flag that
 // makes every CTA leave at its next poll, and the host relaunches the kernel
-// whenever work is pending after it ended. Every wait is bounded (the idle
-// timeout, and kServerMaxPolls polls per wait). Requests and completions live in host-mapped memory; the counters
-// the CTAs poll (published, claimed, stop) live in device memory, so idle
-// CTAs never hammer a host cache line the host is writing.
+// whenever work is pending after it ended. Every wait is bounded: by the
+// idle timeout, by `max_wait_ns` of device time per wait (a host that stops
+// publishing, or never sets the stop flag, frees the SMs within that time),
+// and by kServerMaxPolls polls. Requests and completions live in host-mapped
+// memory; the counters the CTAs poll (published, claimed, stop) live in
+// device memory, so idle CTAs never hammer a host cache line the host is
+// writing.
 constexpr long long kServerMaxPolls = 1LL << 26;
+
+// True once a wait that started at t0 has lasted longer than the server's
+// bound on one wait.
+__device__ __forceinline__ bool server_wait_expired(const ServerArgs& sa, unsigned long long t0,
+                                                    unsigned long long now) {
+  return now > t0 && now - t0 > sa.max_wait_ns;
+}
 
 // One attempt to claim the next published request of a ring (a few CAS
 // retries under contention): its ring index, or -1 when none is waiting.
@@ -208,6 +218,7 @@ __device__ void server_loop(const ServerArgs& sa, Solve solve) {
           atomicExch(sa.closing, 1);
           break;
         }
+        if (server_wait_expired(sa, t0, now)) break;
         __nanosleep(2000);
       }
       atomicSub(sa.idle_ctas, 1);

@@ -596,6 +596,12 @@ mfg_status mfg_batch_create(const mfg_network* nets, const mfg_strategy* strateg
   dv.cur_stress = b->d_cur.p;
   dv.order = b->d_order.p;
   dv.queue = b->d_queue.p;
+  if (b->precision == MFG_PREC_F64) {
+    // Load the module that holds the no-allocation solve's scratch array now,
+    // so that mfg_batch_run_device_noalloc() never reserves it mid-solve.
+    void* scratch = nullptr;
+    MFG_CUDA(mfg::relax_f64_static_scratch_address(&scratch));
+  }
   if (b->precision == MFG_PREC_MIXED) {
     b->mixed.reset(mfg::mixed_new());
     cudaError_t e =
@@ -948,6 +954,7 @@ struct mfg_server {
   cudaStream_t ctrl = nullptr;     // small copies of the published counts and stop flag
   int64_t cap = 0;
   unsigned long long idle_ns = 0;
+  unsigned long long max_wait_ns = 0;
   // lane 0 serves RVEs solved by one CTA; lane 1, when present, the RVEs the
   // mixed serving kernel solves with 4-CTA clusters
   std::vector<ServerLane> lanes;
@@ -1067,6 +1074,7 @@ mfg_status server_lane_create(mfg_server* sv, ServerLane& l) {
   a.closing = sv->ctl_d + 1;
   a.cap = sv->cap;
   a.idle_ns = sv->idle_ns;
+  a.max_wait_ns = sv->max_wait_ns;
   a.sigma = sv->sigma.p;
   a.st_status = sv->st.p;
   a.st_steps = sv->steps.p;
@@ -1096,7 +1104,8 @@ mfg_status mfg_server_create(const mfg_network* nets, const mfg_strategy* strate
   mfg_server_options opt;
   mfg_default_server_options(&opt);
   if (options) opt = *options;
-  if (opt.capacity < 0 || opt.idle_timeout_us < 0 || !(opt.hbm_budget_bytes >= 0))
+  if (opt.capacity < 0 || opt.idle_timeout_us < 0 || !(opt.hbm_budget_bytes >= 0) ||
+      opt.max_wait_ms < 0)
     return fail(MFG_E_INVALID, "negative server option");
   mfg_options bo;
   mfg_default_options(&bo);
@@ -1129,6 +1138,8 @@ mfg_status mfg_server_create(const mfg_network* nets, const mfg_strategy* strate
   sv->cap = opt.capacity > 0 ? opt.capacity : 65536;
   sv->idle_ns = 1000ULL * static_cast<unsigned long long>(opt.idle_timeout_us > 0 ? opt.idle_timeout_us
                                                                                    : 20000);
+  sv->max_wait_ns =
+      1000000ULL * static_cast<unsigned long long>(opt.max_wait_ms > 0 ? opt.max_wait_ms : 5000);
   MFG_CUDA(cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking));
   MFG_CUDA(cudaStreamCreateWithFlags(&sv->ctrl, cudaStreamNonBlocking));
   MFG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&sv->stop_stage), 64, cudaHostAllocDefault));

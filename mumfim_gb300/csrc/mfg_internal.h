@@ -107,6 +107,7 @@ struct ServerArgs {
   ServerDone* done;                 // host-mapped, cap entries
   long long cap;
   unsigned long long idle_ns;
+  unsigned long long max_wait_ns;   // longest a CTA waits for work before it leaves
   double* sigma;                    // device per-RVE scratch, n_rve * 6
   int32_t* st_status;
   int32_t* st_steps;
@@ -128,6 +129,9 @@ struct StaticStatus {
   double* residual;
 };
 size_t relax_f64_static_scratch_bytes(const DevBatch& b, int64_t n_boundary_total);
+// Device address of that array on the current device; the first lookup on a
+// device loads the module that holds it (and so reserves it).
+cudaError_t relax_f64_static_scratch_address(void** addr);
 cudaError_t launch_relax_f64_static(const DevBatch& b, const RunArgs& a, int grid,
                                     int64_t n_boundary_total, cudaStream_t s, StaticStatus* status);
 

@@ -28,7 +28,6 @@
 // giving two block barriers per step.
 #include <cfloat>
 #include <climits>
-#include <mutex>
 
 #include "mumfim_gpu.h"
 
@@ -366,13 +365,21 @@ static __device__ __align__(256) unsigned char g_relax_scratch[MFG_NOALLOC_SCRAT
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_mu;
-void* g_scratch_addr[kMaxDevices] = {};
-
 inline size_t align256(size_t n) { return (n + 255) & ~static_cast<size_t>(255); }
 
 }  // namespace
+
+// Device address of the scratch array on the current device. The host-side
+// symbol is only a stand-in for it. Looking the address up also loads this
+// file's device code on the device if it is not loaded yet (CUDA loads
+// modules lazily), and loading it is what reserves the array, so batch
+// creation calls this once ahead of any solve. The lookup is repeated on
+// every solve rather than cached, so an address never outlives the context
+// it belongs to; once the module is loaded the lookup allocates nothing.
+cudaError_t relax_f64_static_scratch_address(void** addr) {
+  *addr = nullptr;
+  return cudaGetSymbolAddress(addr, g_relax_scratch);
+}
 
 size_t relax_f64_static_scratch_bytes(const DevBatch& b, int64_t n_boundary_total) {
   const size_t R = static_cast<size_t>(b.n_rve);
@@ -388,23 +395,10 @@ cudaError_t launch_relax_f64_static(const DevBatch& batch, const RunArgs& args, 
                                     StaticStatus* status) {
   if (relax_f64_static_scratch_bytes(batch, n_boundary_total) > MFG_NOALLOC_SCRATCH_BYTES)
     return cudaErrorInvalidValue;
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  void* addr = nullptr;
+  cudaError_t e = relax_f64_static_scratch_address(&addr);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  unsigned char* base = nullptr;
-  {
-    // Set-up, once per device, with that device current: the host-side
-    // symbol is only a stand-in; the kernel needs the device address.
-    std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_addr[dev]) {
-      void* p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_relax_scratch);
-      if (e != cudaSuccess) return e;
-      g_scratch_addr[dev] = p;
-    }
-    base = static_cast<unsigned char*>(g_scratch_addr[dev]);
-  }
+  unsigned char* base = static_cast<unsigned char*>(addr);
   const size_t R = static_cast<size_t>(batch.n_rve);
   size_t off = 0;
   auto take = [&](size_t bytes) {

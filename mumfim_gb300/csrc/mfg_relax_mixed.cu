@@ -1177,6 +1177,7 @@ server_cluster_kernel(const DevBatch b, const MixedState ms, const ServerArgs bi
           atomicExch(big.closing, 1);
           break;
         }
+        if (server_wait_expired(big, t0, now)) break;
         __nanosleep(2000);
       }
       atomicSub(big.idle_ctas, 1);

@@ -51,7 +51,7 @@ class RVEServer:
 
     def __init__(self, networks: Sequence, strategies: Sequence, precision: str = "mixed",
                  device: int = 0, capacity: int = 0, idle_timeout_us: int = 0,
-                 hbm_budget_bytes: float = 0.0):
+                 hbm_budget_bytes: float = 0.0, max_wait_ms: int = 0):
         L = _lib()
         self._arr = NetworkArray(networks, strategies)
         o = _abi.mfg_server_options()
@@ -60,6 +60,7 @@ class RVEServer:
         o.capacity = capacity
         o.idle_timeout_us = idle_timeout_us
         o.hbm_budget_bytes = hbm_budget_bytes
+        o.max_wait_ms = max_wait_ms
         h = C.c_void_p()
         _check(L.mfg_server_create(self._arr.nets, self._arr.strats, len(networks), C.byref(o),
                                    C.byref(h)))
@@ -91,12 +92,19 @@ class RVEServer:
         return t.value
 
     def poll(self, max_results: int = 4096, timeout_ms: int = 1000) -> np.ndarray:
+        """Completed results (possibly none). A wait that runs out is not an
+        error here; poll_status() returns the C status as well."""
+        return self.poll_status(max_results, timeout_ms)[0]
+
+    def poll_status(self, max_results: int = 4096, timeout_ms: int = 1000):
+        """(results, mfg_server_poll status): MFG_OK, or MFG_E_TIMEOUT when
+        work is outstanding and nothing completed within timeout_ms."""
         out = np.zeros(max_results, dtype=SERVER_RESULT_DTYPE)
         n = C.c_int32()
         rc = _lib().mfg_server_poll(self._h, out.ctypes.data_as(C.c_void_p), max_results,
                                     C.byref(n), int(timeout_ms))
         _check(rc, allow=(MFG_OK, MFG_E_TIMEOUT))
-        return out[:n.value]
+        return out[:n.value], rc
 
     def drain(self, timeout_s: float = 600.0) -> np.ndarray:
         """Polls until nothing is outstanding; returns every result."""

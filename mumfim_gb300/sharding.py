@@ -8,6 +8,7 @@ come back with one all-gather of (rve id, 6 stresses) rows per call.
 """
 from __future__ import annotations
 
+import datetime
 import heapq
 from typing import List, Sequence
 
@@ -52,3 +53,31 @@ def gather_stress(ids: Sequence[int], sigma: np.ndarray, n_total: int, group=Non
             pid = p[:k, 0].numpy().astype(np.int64)
             out[pid] = p[:k, 1:].numpy()
     return out
+
+
+class RankFailure(RuntimeError):
+    """A rank did not reach a step within the liveness bound."""
+
+    def __init__(self, message: str, missing: Sequence[int]):
+        super().__init__(message)
+        self.missing = list(missing)
+
+
+def await_peers(store, tag: str, rank: int, world: int, timeout_s: float) -> None:
+    """Host-side liveness check between steps, before any rank launches the
+    next solve: every rank announces `tag` in the key-value store (a
+    torch.distributed TCPStore or FileStore) and waits, at most timeout_s, for
+    every other rank's announcement. Raises RankFailure naming the ranks that
+    did not announce, so the survivors stop cleanly instead of blocking in
+    their next collective. The reference has no such check: an MPI rank that
+    dies leaves the others in their next collective."""
+    store.set(f"{tag}/{rank}", b"1")
+    keys = [f"{tag}/{r}" for r in range(world)]
+    try:
+        store.wait(keys, datetime.timedelta(seconds=timeout_s))
+    except Exception as e:
+        missing = [r for r in range(world) if not store.check([f"{tag}/{r}"])]
+        if not missing:
+            raise
+        raise RankFailure(f"ranks {missing} did not reach {tag!r} within {timeout_s} s",
+                          missing) from e

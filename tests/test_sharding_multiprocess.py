@@ -55,6 +55,48 @@ def test_two_rank_sharded_solve_equals_single_process(lib_path, oracle):
         np.testing.assert_array_equal(full, sig)
 
 
+def _liveness_worker(rank, world, port, q):
+    """Step 0 on every rank; rank 2 then dies between steps; the survivors
+    learn of it from the store before step 1 and stop with RankFailure."""
+    import time
+    from datetime import timedelta
+
+    import torch.distributed as dist
+    from mumfim_gb300 import sharding
+    store = dist.TCPStore("127.0.0.1", port, world, rank == 0, timedelta(seconds=60))
+    sharding.await_peers(store, "step0", rank, world, timeout_s=30)
+    if rank == 2:
+        os._exit(3)  # a crashed rank: no cleanup, no goodbye
+    t0 = time.monotonic()
+    try:
+        sharding.await_peers(store, "step1", rank, world, timeout_s=3)
+        q.put((rank, None, time.monotonic() - t0))
+    except sharding.RankFailure as e:
+        q.put((rank, e.missing, time.monotonic() - t0))
+    # the survivors meet once more, so rank 0 keeps the store's server up
+    # until rank 1 is done with it
+    sharding.await_peers(store, "done", rank, 2, timeout_s=30)
+
+
+def test_dead_rank_is_detected_between_steps():
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_liveness_worker, args=(r, 3, port, q)) for r in range(3)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in range(2))
+    for p in procs:
+        p.join(timeout=60)
+    assert procs[2].exitcode == 3
+    assert procs[0].exitcode == 0 and procs[1].exitcode == 0
+    assert [r[0] for r in res] == [0, 1]
+    for rank, missing, waited in res:
+        assert missing == [2]
+        assert waited < 30
+
+
 def test_shard_balance():
     from mumfim_gb300.sharding import shard_rves
     work = [10, 9, 8, 7, 6, 5, 4, 3, 2, 1]
