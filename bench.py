@@ -17,19 +17,34 @@ divided by wall time; RVE solves/s is reported beside it.
   f64_same_batch  the plain FP64 kernel and the mixed kernel on the same
             stratified subset of the batch (every 4th RVE): their throughput
             ratio and the mixed stress error against FP64
-  served    a scaled config-4 stream through the continuous-batching server:
-            persistent RVEs (linear / nonlinear 50/50), load steps x Newton
-            iterations of increments I + U(+-0.005), Poisson arrivals at 80 %
-            of the measured capacity; throughput, p50/p99 latency, and the
+  served_config2  config 2 itself through the continuous-batching server:
+            every RVE one request (its F, 5,000 steps), Poisson arrivals at
+            80 % of the server's saturated throughput on the same requests;
+            throughput over the FP64 kernel's on config 2, p50/p99 latency,
+            and the stress error against the FP64 results of f64_same_batch
+  config3   the nonlinear-law configuration (2048 RVEs, 20,000 steps): mixed
+            throughput on all of it, FP64 on every 16th RVE, the mixed stress
+            error overall and binned by the fraction of an RVE's fibers that
+            end within 0.01 of the toe's transition stretch
+  served_config4  the serving stream at its full 20,000 integration points
+            (linear / nonlinear 50/50), load steps x 3 Newton iterations of
+            increments I + U(+-0.005), 500 steps per request, Poisson arrivals
+            at 80 % of saturation, admission against free HBM; p50/p99 and the
             stress error of a replayed subset against FP64
   roofline  the relaxation kernel's algorithmic bytes (per fiber-step
             20 B + 104 B per node for mixed, 24 B + 108 B per node for FP64)
             over its CUDA-event duration, against the measured HBM bandwidth
+            (a model: the state stays on chip); roofline_binding gives the
+            resource that does bind, the L1TEX (shared memory) pipe and the
+            issue slots, from the committed ncu captures
   cpu_baseline  the CPU oracle (a restatement of the reference's batched
             path: the reference itself needs Kokkos, PUMI, AMSI and MPI and
-            cannot be built) on all host cores, on the first RVEs of the batch
+            cannot be built), its optimised timing build, on all host cores,
+            on the first RVEs of the batch
 
-``--impl reference`` times only that CPU restatement on the same workload.
+``--impl reference`` times only that CPU restatement on the same workload,
+with the network generator taken from the oracle's build directory, so that
+arm maps no library of the product.
 Multi-GPU (torchrun): RVEs are independent; every rank solves its own batch
 of the same shape (weak scaling), no collective touches the data path.
 """
@@ -164,10 +179,15 @@ def rel_err(a, b):
     return float(np.abs(a - b).max() / np.abs(b).max())
 
 
+def _timing_build_desc():
+    from oracle import pyoracle
+    return "g++ " + " ".join(pyoracle.timing_flags())
+
+
 def cpu_baseline(w, sample_rves: int, threads: int):
     from oracle import pyoracle
     sub = w.subset(range(min(sample_rves, w.n_rve)))
-    b = pyoracle.OracleBatch(sub.networks, sub.strategies)
+    b = pyoracle.OracleBatch(sub.networks, sub.strategies, timing=True)
     t0 = time.perf_counter()
     b.run(sub.F, update_coords=False, n_threads=threads)
     dt = time.perf_counter() - t0
@@ -175,7 +195,8 @@ def cpu_baseline(w, sample_rves: int, threads: int):
     return {"value": fs / dt, "unit": "fiber-steps/s", "cores": threads, "kind": "port",
             "sample": f"first {sub.n_rve} RVEs of the workload x {sub.steps} steps "
                       f"({fs:.3g} fiber-steps, {dt:.1f} s; oracle = C++ restatement of the "
-                      f"reference's batched path, -O2 -ffp-contract=off, one RVE per thread)",
+                      f"reference's batched path, timing build {_timing_build_desc()}, one RVE "
+                      f"per thread, {threads} threads)",
             "rve_solves_per_s": sub.n_rve / dt}
 
 
@@ -183,11 +204,13 @@ def run_reference(args, rank, world):
     """CPU restatement of the reference path on the host cores (rank 0 only)."""
     if rank != 0:
         return
+    from mumfim_gb300 import synthetic as S
+    from oracle import pyoracle
+    S.use_netgen_library(pyoracle.build_netgen())
     w, desc = build_workload(args.config, 0, args.n_rve, args.solve_steps, args.nodes)
     threads = os.cpu_count() or 1
-    from oracle import pyoracle
     sub = w.subset(range(min(args.cpu_sample_rves, w.n_rve)))
-    b = pyoracle.OracleBatch(sub.networks, sub.strategies)
+    b = pyoracle.OracleBatch(sub.networks, sub.strategies, timing=True)
     times = []
     for i in range(args.warmup + args.steps):
         t0 = time.perf_counter()
@@ -205,7 +228,8 @@ def run_reference(args, rank, world):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded kNN fiber networks)",
         "config": {"workload": desc, "sample_rves": sub.n_rve, "precision": "f64"},
         "cpu_baseline": {"value": value, "unit": "fiber-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"first {sub.n_rve} RVEs x {sub.steps} steps per step"},
+                         "sample": f"first {sub.n_rve} RVEs x {sub.steps} steps per step; oracle "
+                                   f"timing build {_timing_build_desc()}, one RVE per thread"},
         "e2e": {"value": value, "unit": "fiber-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "rve_solves_per_s": sub.n_rve * len(times) / tot,
@@ -214,118 +238,197 @@ def run_reference(args, rank, world):
 
 
 def f64_same_batch(m, w, every: int):
-    """Plain FP64 and mixed kernels on the same stratified subset."""
-    sub = w.subset(range(0, w.n_rve, every))
+    """Plain FP64 and mixed kernels on the same stratified subset (one solve
+    each; the relaxation kernel's CUDA-event time). Returns the summary and
+    the subset's ids with its FP64 stresses (the served stream's check)."""
+    ids = list(range(0, w.n_rve, every))
+    sub = w.subset(ids)
     out = {}
     sig = {}
     for prec in ("f64", "mixed"):
         g = m.BatchedFiberRVEAnalysisExplicit(sub.networks, sub.strategies, precision=prec)
         s = np.zeros((sub.n_rve, 6))
-        g.run(sub.F, s, update_coords=False)  # warm
         g.run(sub.F, s, update_coords=False)
         relax_ms, _ = g.last_timing()
         out[prec] = sub.total_fibers * sub.steps / (relax_ms * 1e-3)
         sig[prec] = s.copy()
         g.close()
-    return {"subset": f"every {every}th RVE ({sub.n_rve} RVEs, {sub.total_fibers} fibers)",
-            "f64_fiber_steps_per_s": out["f64"], "mixed_fiber_steps_per_s": out["mixed"],
-            "mixed_over_f64": out["mixed"] / out["f64"],
-            "sigma_rel_err_mixed_vs_f64": rel_err(sig["mixed"], sig["f64"])}
+    summary = {"subset": f"every {every}th RVE ({sub.n_rve} RVEs, {sub.total_fibers} fibers)",
+               "f64_fiber_steps_per_s": out["f64"], "mixed_fiber_steps_per_s": out["mixed"],
+               "mixed_over_f64": out["mixed"] / out["f64"],
+               "sigma_rel_err_mixed_vs_f64": rel_err(sig["mixed"], sig["f64"])}
+    return summary, ids, sig["f64"]
 
 
-def saturated_rps(w, n_points: int) -> float:
-    """Requests per second the server completes on this stream when every
-    RVE's request is queued at once (a separate server, so the stream's RVE
-    state is untouched; the second of two rounds is timed)."""
+def serve_stream(m, w, passes, update: bool, rate_frac: float = 0.8):
+    """Runs `passes` (each a list of per-point F) through one server: first
+    one saturation pass of the first pass's requests, all queued at once
+    with update_coords = 0 (in RAMP mode a non-updating solve leaves the
+    state the next solve starts from unchanged), then every pass as a
+    Poisson stream at rate_frac of that throughput. Returns timings,
+    latencies and the stream's stresses per pass."""
     from mumfim_gb300 import synthetic as S
     from mumfim_gb300.serving import RVEServer
-    incs = [S.config4_increment(p, 0, 0) for p in range(n_points)]
-    with RVEServer(w.networks, w.strategies, precision="mixed") as sv:
-        for _ in range(2):
+    n = w.n_rve
+    t_create = time.perf_counter()
+    sv = RVEServer(w.networks, w.strategies, precision="mixed")
+    create_s = time.perf_counter() - t_create
+    try:
+        t0 = time.perf_counter()
+        for p in range(n):
+            sv.submit(p, passes[0][p], update_coords=False)
+        done = 0
+        while done < n:
+            done += len(sv.poll(timeout_ms=50))
+        sat_s = time.perf_counter() - t0
+        rate = rate_frac * n / sat_s
+        lat, dev = [], []
+        sigma = [np.zeros((n, 6)) for _ in passes]
+        status_ok = True
+        t_start = time.perf_counter()
+        for k, Fk in enumerate(passes):
+            arrivals = S.poisson_arrivals(1000 + k, n, rate)
+            order = np.argsort(S.uniform(7 + k, n))
             t0 = time.perf_counter()
-            for p in range(n_points):
-                sv.submit(p, incs[p], update_coords=False)
-            done = 0
-            while done < n_points:
-                done += len(sv.poll(timeout_ms=50))
-            t = time.perf_counter() - t0
-    return n_points / t
-
-
-def served(m, n_points: int, load_steps: int, iters: int, steps: int, check: int):
-    """Scaled config-4 stream through the continuous-batching server, offered
-    at 80 % of the server's saturated throughput on the same stream."""
-    from mumfim_gb300 import synthetic as S
-    from mumfim_gb300.serving import RVEServer
-    w = S.config4(n_points=n_points, steps=steps)
-    fib = np.array([n.n_fibers for n in w.networks], dtype=np.float64)
-    capacity_rps = saturated_rps(w, n_points)
-    rate = 0.8 * capacity_rps  # requests per second
-    lat, dev = [], []
-    hist = {}  # point -> list of sigma per request (checked subset)
-    t_start = None
-    n_done = 0
-    with RVEServer(w.networks, w.strategies, precision="mixed") as sv:
-        for ls in range(load_steps):
-            for it in range(iters):
-                arrivals = S.poisson_arrivals(1000 * ls + it, n_points, rate)
-                order = np.argsort(S.uniform(7 + 1000 * ls + it, n_points))
-                t0 = time.perf_counter()
-                if t_start is None:
-                    t_start = t0
-                incs = [S.config4_increment(p, ls, it) for p in range(n_points)]
-                k = 0
-                pending = 0
-                while k < n_points or pending > 0:
-                    now = time.perf_counter() - t0
-                    while k < n_points and arrivals[k] <= now:
-                        p = int(order[k])
-                        sv.submit(p, incs[p], update_coords=True)
-                        k += 1
-                        pending += 1
-                    res = sv.poll(timeout_ms=0 if k < n_points else 50)
-                    pending -= len(res)
-                    n_done += len(res)
-                    lat.extend(res["latency_s"].tolist())
-                    dev.extend(res["device_s"].tolist())
-                    for rec in res:
-                        if rec["rve"] < check:
-                            hist.setdefault(int(rec["rve"]), []).append(rec["sigma"].copy())
-                    if k < n_points:
-                        time.sleep(min(max(arrivals[k] - (time.perf_counter() - t0), 0), 0.0005))
+            i = pending = 0
+            while i < n or pending > 0:
+                now = time.perf_counter() - t0
+                while i < n and arrivals[i] <= now:
+                    p = int(order[i])
+                    sv.submit(p, Fk[p], update_coords=update)
+                    i += 1
+                    pending += 1
+                res = sv.poll(timeout_ms=0 if i < n else 50)
+                pending -= len(res)
+                lat.extend(res["latency_s"].tolist())
+                dev.extend(res["device_s"].tolist())
+                if len(res):
+                    sigma[k][res["rve"]] = res["sigma"]
+                    status_ok = status_ok and bool((res["status"] == 0).all())
+                if i < n:
+                    time.sleep(min(max(arrivals[i] - (time.perf_counter() - t0), 0), 0.0005))
         wall = time.perf_counter() - t_start
         launches = sv.launches()
-    # replay the checked points on the plain FP64 kernel
+    finally:
+        sv.close()
+    lat = np.array(lat)
+    return {"create_s": create_s, "saturated_rve_solves_per_s": n / sat_s,
+            "offered_rate_per_s": rate, "requests": int(len(lat)), "wall_s": wall,
+            "latency_p50_ms": float(np.percentile(lat, 50) * 1e3),
+            "latency_p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "device_p50_ms": float(np.percentile(dev, 50) * 1e3),
+            "kernel_launches": int(launches), "all_ok": status_ok}, sigma
+
+
+def served_config2(m, w, f64_ids, f64_sigma, f64_rate):
+    """Config 2 itself as a served stream: one request per RVE (its F, the
+    batch's 5,000 steps, update_coords = 0, the same work as a bench step),
+    against the FP64 kernel's rate and stresses on the same batch."""
+    r, sigma = serve_stream(m, w, [list(w.F)], update=False)
+    fs = float(w.total_fibers) * w.steps
+    r["fiber_steps_per_s"] = fs / r["wall_s"]
+    r["rve_solves_per_s"] = w.n_rve / r["wall_s"]
+    r["served_over_f64"] = r["fiber_steps_per_s"] / f64_rate
+    r["sigma_rel_err_vs_f64"] = rel_err(sigma[0][f64_ids], f64_sigma)
+    r["workload"] = (f"config2: all {w.n_rve} RVEs, one request each ({w.steps} ramp steps), "
+                     f"Poisson arrivals at 80 % of the server's saturated throughput; FP64 "
+                     f"rate and stresses from f64_same_batch ({len(f64_ids)} RVEs of the batch)")
+    return r
+
+
+def served_config4(m, n_points: int, load_steps: int, iters: int, steps: int, check: int):
+    """The config-4 serving stream: n_points persistent RVEs, load_steps x
+    iters updating increments per point, Poisson arrivals at 80 % of
+    saturation; the first `check` points replayed on the FP64 kernel."""
+    from mumfim_gb300 import synthetic as S
+    t0 = time.perf_counter()
+    w = S.config4(n_points=n_points, steps=steps)
+    gen_s = time.perf_counter() - t0
+    passes = [[S.config4_increment(p, ls, it) for p in range(n_points)]
+              for ls in range(load_steps) for it in range(iters)]
+    r, sigma = serve_stream(m, w, passes, update=True)
+    fs = float(w.total_fibers) * steps * len(passes)
+    r["fiber_steps_per_s"] = fs / r["wall_s"]
+    r["rve_solves_per_s"] = r["requests"] / r["wall_s"]
     sub = w.subset(range(check))
     g = m.BatchedFiberRVEAnalysisExplicit(sub.networks, sub.strategies, precision="f64")
     errs = []
-    for ls in range(load_steps):
-        for it in range(iters):
-            F = np.stack([S.config4_increment(p, ls, it) for p in range(check)])
-            s = np.zeros((check, 6))
-            g.run(F, s, update_coords=True)
-            j = ls * iters + it
-            got = np.stack([hist[p][j] for p in range(check)])
-            errs.append(rel_err(got, s))
+    for k, Fk in enumerate(passes):
+        s = np.zeros((check, 6))
+        g.run(np.stack(Fk[:check]), s, update_coords=True)
+        errs.append(rel_err(sigma[k][:check], s))
     g.close()
-    total_fs = float(fib.sum()) * steps * load_steps * iters
-    lat = np.array(lat)
-    return {
-        "workload": (f"config4 scaled: {n_points} persistent RVEs (of 20,000), nodes log-uniform "
-                     f"[500,20000], linear/nonlinear 50/50, {load_steps} load steps x {iters} Newton "
-                     f"iterations, increments I + U(+-0.005), {steps} ramp steps per request, "
-                     f"Poisson arrivals at {rate:.0f}/s (80 % of the server's saturated "
-                     f"throughput on this stream)"),
-        "saturated_rve_solves_per_s": capacity_rps,
-        "requests": int(n_done), "wall_s": wall,
-        "fiber_steps_per_s": total_fs / wall, "rve_solves_per_s": n_done / wall,
-        "latency_p50_ms": float(np.percentile(lat, 50) * 1e3),
-        "latency_p99_ms": float(np.percentile(lat, 99) * 1e3),
-        "device_p50_ms": float(np.percentile(dev, 50) * 1e3),
-        "kernel_launches": int(launches),
-        "sigma_rel_err_vs_f64": float(max(errs)),
-        "checked_points": check,
-    }
+    r["sigma_rel_err_vs_f64"] = float(max(errs))
+    r["checked_points"] = check
+    r["generate_s"] = gen_s
+    r["workload"] = (f"config4: {n_points} persistent RVEs (integration points), nodes log-uniform "
+                     f"[500,20000], k in {{3,4,5}}, linear/nonlinear 50/50, {load_steps} load "
+                     f"steps x {iters} Newton iterations (of the configuration's 50 x 3), "
+                     f"increments I + U(+-0.005), {steps} ramp steps per request, Poisson "
+                     f"arrivals at 80 % of saturation, admission against free HBM")
+    return r
+
+
+def config3_section(m, every: int):
+    """Config 3 as specified: mixed throughput on the whole batch, FP64 on
+    every `every`-th RVE, and the mixed stress error against FP64 -- overall
+    and by how many of an RVE's fibers end near the toe's transition stretch
+    (|lambda - lambda_t| <= 0.01, lambda from the FP64 solve's final
+    coordinates)."""
+    from mumfim_gb300 import synthetic as S
+    w = S.config3()
+    g = m.BatchedFiberRVEAnalysisExplicit(w.networks, w.strategies, precision="mixed")
+    s_all = np.zeros((w.n_rve, 6))
+    g.run(w.F, s_all, update_coords=False)
+    mixed_ms, _ = g.last_timing()
+    g.close()
+    ids = list(range(0, w.n_rve, every))
+    sub = w.subset(ids)
+    g = m.BatchedFiberRVEAnalysisExplicit(sub.networks, sub.strategies, precision="f64")
+    s64 = np.zeros((sub.n_rve, 6))
+    g.run(sub.F, s64, update_coords=False)
+    f64_ms, _ = g.last_timing()
+    near = np.zeros(sub.n_rve)
+    for r, net in enumerate(sub.networks):
+        x = g.coordinates(r)
+        c = net.connectivity
+        lam = (np.linalg.norm(x[c[:, 1]] - x[c[:, 0]], axis=1)
+               / np.linalg.norm(net.coords[c[:, 1]] - net.coords[c[:, 0]], axis=1))
+        near[r] = float(np.mean(np.abs(lam - net.reactions[0].length_ratio_trns) <= 0.01))
+    g.close()
+    sm = s_all[ids]
+    err = np.abs(sm - s64).max(axis=1) / np.abs(s64).max(axis=1)
+    q = np.quantile(near, [0.0, 0.25, 0.5, 0.75, 1.0])
+    bins = []
+    for lo, hi in zip(q[:-1], q[1:]):
+        sel = (near >= lo) & (near <= hi)
+        bins.append({"near_toe_frac": [float(lo), float(hi)], "rves": int(sel.sum()),
+                     "max_rel_err": float(err[sel].max())})
+    return {"workload": f"config3: {w.n_rve} RVEs, nodes log-uniform [2000,8000], "
+                        f"exponential-toe law, {w.steps} ramp steps",
+            "mixed_fiber_steps_per_s": w.total_fibers * w.steps / (mixed_ms * 1e-3),
+            "f64_fiber_steps_per_s": sub.total_fibers * sub.steps / (f64_ms * 1e-3),
+            "f64_subset": f"every {every}th RVE ({sub.n_rve} RVEs)",
+            "sigma_rel_err_mixed_vs_f64": float(err.max()),
+            "near_toe_frac_mean": float(near.mean()),
+            "err_by_near_toe_quartile": bins}
+
+
+def roofline_binding():
+    """Time-weighted L1TEX pipe and issue-slot fractions of the mixed
+    kernel's size buckets, from the committed ncu captures."""
+    p = os.path.join(REPO, "profiles", "binding_config2_mixed.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as fh:
+        d = json.load(fh)
+    b = d["buckets"]
+    tot = sum(v["time_share"] for v in b.values())
+    l1 = sum(v["time_share"] * v["l1tex_pipe_frac"] for v in b.values()) / tot
+    iss = sum(v["time_share"] * v["issue_slots_frac"] for v in b.values()) / tot
+    return {"resource": "L1TEX pipe (shared and distributed shared memory)", "frac": l1,
+            "issue_slots_frac": iss, "unit": "fraction of peak, ncu, time-weighted over buckets",
+            "source": "profiles/binding_config2_mixed.json"}
 
 
 def main():
@@ -343,14 +446,18 @@ def main():
     ap.add_argument("--nodes", default=None, metavar="LO:HI",
                     help="config 2 with node counts log-uniform in [LO, HI] (profiling cases)")
     ap.add_argument("--f64-every", type=int, default=4)
-    ap.add_argument("--serve-points", type=int, default=2048)
+    ap.add_argument("--serve-points", type=int, default=20_000,
+                    help="integration points of the config-4 stream")
+    ap.add_argument("--serve-load-steps", type=int, default=1,
+                    help="load steps of the config-4 stream (3 Newton iterations each)")
     ap.add_argument("--serve-steps", type=int, default=500)
+    ap.add_argument("--config3-every", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--autotune", action="store_true",
                     help="mixed: time 100-step solves under each cluster-size limit first and "
                          "use the fastest (mumfim_gb300.autotune)")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the FP64 side-by-side and the served stream")
+                    help="skip the FP64 side-by-side, the served streams and config 3")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
@@ -488,9 +595,18 @@ def main():
     }
     if clk:
         line["clocks"] = clk
+    binding = roofline_binding() if args.precision == "mixed" else None
+    if binding:
+        line["roofline_binding"] = binding
     if rank == 0 and world == 1 and not args.no_extras:
-        line["f64_same_batch"] = f64_same_batch(m, w, args.f64_every)
-        line["served"] = served(m, args.serve_points, 2, 3, args.serve_steps, 32)
+        summary, ids, s64 = f64_same_batch(m, w, args.f64_every)
+        line["f64_same_batch"] = summary
+        if args.config == 2 and args.precision == "mixed":
+            line["served_config2"] = served_config2(m, w, ids, s64,
+                                                    summary["f64_fiber_steps_per_s"])
+        line["config3"] = config3_section(m, args.config3_every)
+        line["served_config4"] = served_config4(m, args.serve_points, args.serve_load_steps, 3,
+                                                args.serve_steps, 32)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, args.cpu_sample_rves, os.cpu_count() or 1)
     if rank == 0:

@@ -123,8 +123,33 @@ typedef struct mfg_options {
                                places RVEs that need a cluster on clusters of 4
                                (never 2), the size the serving kernel solves in
                                clusters; the results are the same either way. */
-  int32_t reserved[3];
+  int32_t stiffness;        /* mfg_stiffness_solves: how mfg_batch_material_stiffness()
+                               runs its six perturbed solves */
+  int32_t reserved[2];
 } mfg_options;
+
+/* The six perturbed solves of mfg_batch_material_stiffness(). The reference
+ * runs them as six whole-batch runs one after the other
+ * (BatchedFiberRVEAnalysisExplicit.h:321-405), and each non-updating run
+ * leaves its relaxed current coordinates behind (it restores only the
+ * displacement), which the next run's affine predictor starts from. In RAMP
+ * mode nothing reads those coordinates, so the six solves are independent.
+ *  CONCURRENT   all six solves of every RVE in flight at once (six sets of
+ *               per-solve scratch, 6 x the FP64 node and fiber work arrays),
+ *               each starting from the state of the last updating run; the
+ *               current coordinates end as the sixth solve leaves them. In
+ *               RAMP mode this gives the sequential results bit for bit; in
+ *               RELAX mode each predictor starts from the last updating
+ *               run's coordinates instead of the previous perturbation's, so
+ *               results differ within the relaxation tolerance.
+ *  SEQUENTIAL   the reference's order, in every mode.
+ *  AUTO         CONCURRENT when every RVE of the batch is in RAMP mode (where
+ *               it is exact), else SEQUENTIAL. */
+typedef enum mfg_stiffness_solves {
+  MFG_STIFFNESS_AUTO = 0,
+  MFG_STIFFNESS_SEQUENTIAL = 1,
+  MFG_STIFFNESS_CONCURRENT = 2
+} mfg_stiffness_solves;
 
 typedef enum mfg_cluster_layout {
   MFG_LAYOUT_BATCH = 0,   /* smallest of 1, 2, 4, 8 CTAs that holds the RVE */
@@ -316,20 +341,23 @@ typedef struct mfg_server_options {
   int32_t reserved[3];
 } mfg_server_options;
 
-/* One completed request. sigma maps onto micro_fo_result.data[0..5]
- * (MultiscaleMicroFOParams.h:93-98). */
+/* One completed request. sigma maps onto micro_fo_result.data[0..5] and C
+ * onto micro_fo_result.data[9..44] (MultiscaleMicroFOParams.h:93-98). */
 typedef struct mfg_server_result {
   int64_t ticket;
   int32_t rve;
   int32_t status;  /* MFG_OK, MFG_E_NOT_CONVERGED or MFG_E_NONFINITE */
   int32_t steps;
-  int32_t pad_;
+  int32_t stiffness_status;  /* worst status of the six perturbed solves; -1 when the
+                                request did not ask for the stiffness */
   double residual;
   double sigma[6];
   double latency_s;  /* submit -> result seen by mfg_server_poll, host clock */
-  double device_s;   /* claim -> completion on the device */
+  double device_s;   /* claim -> completion on the device (stiffness solves included) */
   int64_t t_claim_ns;  /* device %globaltimer when a CTA claimed the request */
   int64_t t_done_ns;   /* device %globaltimer when its result was published */
+  double C[36];        /* material stiffness C[6 j + i] as mfg_batch_material_stiffness()
+                          returns it (zeros unless requested) */
 } mfg_server_result;
 
 void mfg_default_server_options(mfg_server_options* out);
@@ -341,6 +369,17 @@ mfg_status mfg_server_create(const mfg_network* nets, const mfg_strategy* strate
  * micro_fo_data.data). Non-blocking. MFG_E_BUSY when the ring is full. */
 mfg_status mfg_server_submit(mfg_server* server, int32_t rve, const double* F,
                              int32_t update_coords, int64_t* ticket);
+/* As mfg_server_submit(); with `stiffness` nonzero the request also returns
+ * the RVE's material stiffness, the one computeMaterialStiffness(C) gives
+ * after run() in the reference's service loop (MultiscaleRVEAnalysis.cc:257-258;
+ * BatchedFiberRVEAnalysisExplicit.h:321-405): right after the request's own
+ * solve the CTA (or cluster) that ran it runs the six perturbed,
+ * non-updating solves in the reference's order, around the stress of the
+ * RVE's last updating run. Stress and stiffness together make a full
+ * micro_fo_result, bit-identical to mfg_batch_run() followed by a
+ * sequential mfg_batch_material_stiffness() on the same RVE. */
+mfg_status mfg_server_submit_ex(mfg_server* server, int32_t rve, const double* F,
+                                int32_t update_coords, int32_t stiffness, int64_t* ticket);
 /* Returns up to `capacity` completed requests, waiting up to timeout_ms for
  * the first one. MFG_E_TIMEOUT when work is outstanding and none completed. */
 mfg_status mfg_server_poll(mfg_server* server, mfg_server_result* out, int32_t capacity,

@@ -28,6 +28,7 @@ MFG_MODE_RELAX = 0
 MFG_MODE_RAMP = 1
 MFG_PREC_F64 = 0
 MFG_PREC_MIXED = 1
+MFG_STIFFNESS = {"auto": 0, "sequential": 1, "concurrent": 2}
 
 
 class mfg_reaction(C.Structure):
@@ -50,7 +51,8 @@ class mfg_strategy(C.Structure):
 class mfg_options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("device", C.c_int32),
                 ("threads_per_rve", C.c_int32), ("max_cluster_ctas", C.c_int32),
-                ("cluster_layout", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("cluster_layout", C.c_int32), ("stiffness", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
 
 class mfg_rve_status(C.Structure):
@@ -102,7 +104,8 @@ class mfg_server_options(C.Structure):
 
 
 SERVER_RESULT_DTYPE = np.dtype([("ticket", np.int64), ("rve", np.int32), ("status", np.int32),
-                                ("steps", np.int32), ("pad_", np.int32), ("residual", np.float64),
-                                ("sigma", np.float64, (6,)), ("latency_s", np.float64),
-                                ("device_s", np.float64), ("t_claim_ns", np.int64),
-                                ("t_done_ns", np.int64)])
+                                ("steps", np.int32), ("stiffness_status", np.int32),
+                                ("residual", np.float64), ("sigma", np.float64, (6,)),
+                                ("latency_s", np.float64), ("device_s", np.float64),
+                                ("t_claim_ns", np.int64), ("t_done_ns", np.int64),
+                                ("C", np.float64, (6, 6))])

@@ -115,10 +115,14 @@ class BatchedFiberRVEAnalysisExplicit:
                 split over (1, 2, 4 or 8; 0 = 8); results do not depend on it
     serving_layout  mixed precision: RVEs that need a cluster get clusters of 4
                 (never 2), the layout the serving kernel uses; same results
+    stiffness   "auto", "sequential" or "concurrent": how computeMaterialStiffness
+                runs its six perturbed solves (mfg_stiffness_solves in
+                include/mumfim_gpu.h)
     """
 
     def __init__(self, networks: Sequence, strategies: Sequence, precision: str = "f64",
-                 device: int = 0, max_cluster_ctas: int = 0, serving_layout: bool = False):
+                 device: int = 0, max_cluster_ctas: int = 0, serving_layout: bool = False,
+                 stiffness: str = "auto"):
         L = load_library()
         if len(networks) != len(strategies):
             raise ValueError("There must be a solution strategy for each fiber network!")
@@ -128,6 +132,7 @@ class BatchedFiberRVEAnalysisExplicit:
         opts.device = device
         opts.max_cluster_ctas = max_cluster_ctas
         opts.cluster_layout = 1 if serving_layout else 0
+        opts.stiffness = _abi.MFG_STIFFNESS[stiffness]
         h = C.c_void_p()
         _check(L.mfg_batch_create(self._arr.nets, self._arr.strats, len(networks), C.byref(opts),
                                   C.byref(h)))

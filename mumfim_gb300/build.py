@@ -1,4 +1,6 @@
-"""Builds libmumfim_gpu.so in-tree (mumfim_gb300/_lib/) for sm_103a.
+"""Builds libmumfim_gpu.so in-tree (mumfim_gb300/_lib/) for sm_103a, and
+libmumfim_netgen.so, the seeded synthetic-network generator of the tests and
+benchmarks (host code only, kept out of the solver library).
 
 Every translation unit is compiled in parallel; the CUDA ones with
 ``-gencode arch=compute_103a,code=sm_103a``. Host code and the bit-exact FP64
@@ -24,13 +26,14 @@ OUT_DIR = os.path.join(PKG, "_lib")
 OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB_NAME = "libmumfim_gpu.so"
 LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
+NETGEN_PATH = os.path.join(OUT_DIR, "libmumfim_netgen.so")
+NETGEN_SRC = os.path.join(CSRC, "netgen.cpp")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 # (source, kind, extra flags)
 SOURCES = [
     ("mfg_host.cpp", "cxx", []),
-    ("netgen.cpp", "cxx", []),
     ("mfg_coupling.cpp", "cxx", []),
     ("mfg_mixed_order.cpp", "cxx", []),
     ("mfg_relax_f64.cu", "cuda", ["--fmad=false"]),
@@ -78,16 +81,38 @@ def _compile(src: str, kind: str, extra: list[str], cuda: str, newest_header: fl
     return obj
 
 
+def build_netgen(out_path: str = NETGEN_PATH, force: bool = False) -> str:
+    """Compiles the network generator (netgen.cpp, IEEE +-*/ only, no
+    contraction: the same networks on every platform) into its own shared
+    library at out_path; returns the path."""
+    deps = [NETGEN_SRC, os.path.join(INCLUDE, "mumfim_netgen.h"), __file__]
+    if (not force and os.path.exists(out_path)
+            and os.path.getmtime(out_path) >= max(os.path.getmtime(d) for d in deps)):
+        return out_path
+    os.makedirs(os.path.dirname(out_path), exist_ok=True)
+    tmp = out_path + ".tmp"
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-Wall",
+           "-I" + INCLUDE, NETGEN_SRC, "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compiling netgen.cpp failed:\n{' '.join(cmd)}\n{r.stderr}")
+    os.replace(tmp, out_path)
+    return out_path
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
-    """Compiles (incrementally) and links the library; returns its path."""
+    """Compiles (incrementally) and links the library and the network
+    generator; returns the library's path."""
     os.makedirs(OBJ_DIR, exist_ok=True)
     cuda = _cuda_home()
     newest = max(os.path.getmtime(h) for h in _headers())
     if force:
         for f in os.listdir(OBJ_DIR):
             os.remove(os.path.join(OBJ_DIR, f))
-    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+    with ThreadPoolExecutor(max_workers=len(SOURCES) + 1) as ex:
+        ng = ex.submit(build_netgen, NETGEN_PATH, force)
         objs = list(ex.map(lambda s: _compile(s[0], s[1], s[2], cuda, newest), SOURCES))
+        ng.result()
     if (not os.path.exists(LIB_PATH)
             or os.path.getmtime(LIB_PATH) < max(os.path.getmtime(o) for o in objs)):
         tmp = LIB_PATH + ".tmp"

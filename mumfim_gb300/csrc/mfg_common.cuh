@@ -167,13 +167,16 @@ __device__ __forceinline__ void server_read_request(const ServerArgs& sa, long l
   __threadfence_system();  // order the ring entry after the tail we saw
   const volatile ServerReq* q = sa.ring + (idx % sa.cap);
   s_req[0] = ld_sys(&q->rve);
-  s_req[1] = ld_sys(&q->update_coords);
+  s_req[1] = ld_sys(&q->flags);
   for (int k = 0; k < 9; ++k) s_F[k] = ld_sys(&q->F[k]);
 }
 
-// Publishes the completion record of request `idx` (one thread).
+// Publishes the completion record of request `idx` (one thread); with
+// `stiffness`, also the RVE's material stiffness and the worst status of its
+// perturbed solves.
 __device__ __forceinline__ void server_publish_done(const ServerArgs& sa, long long idx, int rve,
-                                                    unsigned long long t_claim) {
+                                                    unsigned long long t_claim,
+                                                    bool stiffness = false) {
   __threadfence();
   volatile ServerDone* d = sa.done + (idx % sa.cap);
   st_sys(&d->rve, rve);
@@ -181,10 +184,42 @@ __device__ __forceinline__ void server_publish_done(const ServerArgs& sa, long l
   st_sys(&d->steps, sa.st_steps[rve]);
   st_sys(&d->residual, sa.st_residual[rve]);
   for (int k = 0; k < 6; ++k) st_sys(&d->sigma[k], sa.sigma[6 * rve + k]);
+  st_sys(&d->stiff_status, stiffness ? sa.stiff_status[rve] : -1);
+  if (stiffness)
+    for (int k = 0; k < 36; ++k) st_sys(&d->C[k], sa.C[36 * rve + k]);
   st_sys(&d->t_claim_ns, static_cast<long long>(t_claim));
   st_sys(&d->t_done_ns, static_cast<long long>(global_ns()));
   __threadfence_system();
   st_release_sys(&d->ticket_plus1, idx + 1);
+}
+
+// Arguments of perturbed solve i of a request's material stiffness: the
+// i-th perturbation gradient, no update, results into the stiffness scratch.
+__device__ __forceinline__ RunArgs stiffness_args(const ServerArgs& sa, int i) {
+  RunArgs a;
+  a.F = sa.stiff_F + 9 * i;
+  a.n_F = 1;
+  a.update_coords = 0;
+  a.sigma = sa.sigma1;
+  a.st_status = sa.st1_status;
+  a.st_steps = sa.st1_steps;
+  a.st_residual = sa.st1_residual;
+  return a;
+}
+
+// Column i of the RVE's stiffness from perturbed solve i, C[j][i] =
+// (sigma_i[j] - sigma[j]) / h around the stress of the last updating run
+// (BatchedFiberRVEAnalysisExplicit.h:396-403), and the worst perturbed
+// status; threads 0-5 of the CTA that holds the stress. The caller
+// separates successive calls with a barrier.
+__device__ __forceinline__ void stiffness_column(const ServerArgs& sa, int rve, int i) {
+  const int j = threadIdx.x;
+  if (j < 6)
+    sa.C[36 * rve + 6 * j + i] = (sa.sigma1[6 * rve + j] - sa.cur_stress[6 * rve + j]) / kStiffStep;
+  if (j == 0) {
+    const int st = sa.st1_status[rve];
+    sa.stiff_status[rve] = i == 0 ? st : max(sa.stiff_status[rve], st);
+  }
 }
 
 template <typename Solve>
@@ -228,20 +263,30 @@ __device__ void server_loop(const ServerArgs& sa, Solve solve) {
     __syncthreads();
     const long long idx = s_idx;
     const int rve = s_req[0];
-    const int update = s_req[1];
+    const int flags = s_req[1];
     __syncthreads();
     if (idx < 0) return;
     const unsigned long long t_claim = global_ns();
     RunArgs a;
     a.F = s_F;
     a.n_F = 1;
-    a.update_coords = update;
+    a.update_coords = flags & kReqUpdate;
     a.sigma = sa.sigma;
     a.st_status = sa.st_status;
     a.st_steps = sa.st_steps;
     a.st_residual = sa.st_residual;
-    solve(a, rve);  // ends with __syncthreads()
-    if (threadIdx.x == 0) server_publish_done(sa, idx, rve, t_claim);
+    // the request's solve, then with kReqStiffness the six perturbed solves
+    // of mfg_batch_material_stiffness(), in its order, on this CTA (one call
+    // site, so the solve is inlined once)
+    const bool stiff = (flags & kReqStiffness) != 0;
+    for (int k = 0; k <= (stiff ? 6 : 0); ++k) {
+      solve(k == 0 ? a : stiffness_args(sa, k - 1), rve);  // ends with __syncthreads()
+      if (k > 0) {
+        stiffness_column(sa, rve, k - 1);
+        __syncthreads();
+      }
+    }
+    if (threadIdx.x == 0) server_publish_done(sa, idx, rve, t_claim, stiff);
     __syncthreads();
   }
 }

@@ -255,6 +255,57 @@ struct DevArray {
   }
 };
 
+// Scratch of the concurrent perturbed solves of the material stiffness: six
+// sets of every array a non-updating run writes (coordinates, velocities,
+// internal forces, force vectors, RAMP data, stresses, status words, work
+// counter), allocated on first use and kept with the batch.
+constexpr int kStiffSlots = 6;
+struct StiffSlots {
+  bool ready = false;
+  DevArray<double> x, v, fint, nrm, ramp, sigma, res, F;
+  DevArray<int32_t> status, steps, queue;
+  cudaStream_t st[kStiffSlots] = {};
+  cudaEvent_t fork = nullptr, join[kStiffSlots] = {};
+  void release() {
+    for (auto* a : {&x, &v, &fint, &nrm, &ramp, &sigma, &res, &F}) a->release();
+    for (auto* a : {&status, &steps, &queue}) a->release();
+    for (int k = 0; k < kStiffSlots; ++k) {
+      if (st[k]) cudaStreamDestroy(st[k]);
+      if (join[k]) cudaEventDestroy(join[k]);
+      st[k] = nullptr;
+      join[k] = nullptr;
+    }
+    if (fork) cudaEventDestroy(fork);
+    fork = nullptr;
+    ready = false;
+  }
+};
+
+// The six perturbation gradients of the FD stiffness, row-major, h = 1e-5
+// (BatchedFiberRVEAnalysisExplicit.h:331-395).
+constexpr double kStiffH = 1E-5;
+void perturbation_gradients(double Fa[kStiffSlots][9]) {
+  constexpr double h = kStiffH;
+  double D1 = std::sqrt(1.0 / (1 - 2 * h));
+  constexpr double l1 = 1;
+  constexpr double l2 = (1 + h) / (1 - h * h);
+  constexpr double l3 = (1 - h) / (1 - h * h);
+  double l2pl3 = 0.5 * (std::sqrt(l2) + std::sqrt(l3));
+  double l2ml3 = 0.5 * (std::sqrt(l2) - std::sqrt(l3));
+  for (int i = 0; i < kStiffSlots; ++i) {
+    double* F = Fa[i];
+    for (int k = 0; k < 9; ++k) F[k] = 0;
+    switch (i) {
+      case 0: F[0] = D1; F[4] = 1; F[8] = 1; break;
+      case 1: F[0] = 1; F[4] = D1; F[8] = 1; break;
+      case 2: F[0] = 1; F[4] = 1; F[8] = D1; break;
+      case 3: F[0] = l1; F[4] = l2pl3; F[8] = l2pl3; F[5] = l2ml3; F[7] = l2ml3; break;
+      case 4: F[0] = l2pl3; F[4] = l1; F[8] = l2pl3; F[2] = l2ml3; F[6] = l2ml3; break;
+      default: F[0] = l2pl3; F[4] = l2pl3; F[8] = l1; F[1] = l2ml3; F[3] = l2ml3; break;
+    }
+  }
+}
+
 }  // namespace
 
 struct mfg_batch {
@@ -281,9 +332,13 @@ struct mfg_batch {
   DevArray<mfg_rve_status> d_st;
   mfg::DevBatch dev{};
   std::unique_ptr<mfg::MixedState, mfg::MixedStateDeleter> mixed;
+  int stiffness = MFG_STIFFNESS_AUTO;
+  bool all_ramp = false;
+  StiffSlots stiff;
 
   ~mfg_batch() {
     if (device >= 0) cudaSetDevice(device);
+    stiff.release();
     mixed.reset();
     for (auto* a : {&d_X, &d_x, &d_u, &d_v, &d_m, &d_l0, &d_nrm, &d_fint, &d_ramp, &d_vol, &d_cur,
                     &d_F, &d_sigma, &d_res, &d_omega})
@@ -431,6 +486,10 @@ mfg_status mfg_batch_create(const mfg_network* nets, const mfg_strategy* strateg
   if (opt.cluster_layout != MFG_LAYOUT_BATCH && opt.cluster_layout != MFG_LAYOUT_SERVING)
     return fail(MFG_E_INVALID, "cluster_layout must be MFG_LAYOUT_BATCH or MFG_LAYOUT_SERVING "
                 "(got %d)", opt.cluster_layout);
+  if (opt.stiffness != MFG_STIFFNESS_AUTO && opt.stiffness != MFG_STIFFNESS_SEQUENTIAL &&
+      opt.stiffness != MFG_STIFFNESS_CONCURRENT)
+    return fail(MFG_E_INVALID, "stiffness must be MFG_STIFFNESS_AUTO, _SEQUENTIAL or _CONCURRENT "
+                "(got %d)", opt.stiffness);
   for (int r = 0; r < n_rve; ++r) {
     mfg_status st = check_strategy(strategies[r], r);
     if (st != MFG_OK) return st;
@@ -461,6 +520,9 @@ mfg_status mfg_batch_create(const mfg_network* nets, const mfg_strategy* strateg
   std::unique_ptr<mfg_batch> b(new mfg_batch());
   b->device = opt.device;
   b->precision = opt.precision;
+  b->stiffness = opt.stiffness;
+  b->all_ramp = true;
+  for (int r = 0; r < n_rve; ++r) b->all_ramp = b->all_ramp && strategies[r].mode == MFG_MODE_RAMP;
   b->R = n_rve;
   b->sms = prop.multiProcessorCount;
   b->n_nodes.resize(n_rve);
@@ -730,38 +792,147 @@ mfg_status mfg_batch_run(mfg_batch* b, const double* F, int32_t n_F, double* sig
   return static_cast<mfg_status>(worst);
 }
 
+}  // extern "C"
+
+namespace {
+
+// Allocates the concurrent stiffness solves' scratch on first use.
+mfg_status stiff_slots_ready(mfg_batch* b) {
+  StiffSlots& sl = b->stiff;
+  if (sl.ready) return MFG_OK;
+  const size_t K = kStiffSlots, nt = b->nt, et = b->et, R = b->R;
+  const size_t nbt = std::max<int64_t>(b->nbt, 1);
+  cudaError_t e = cudaSuccess;
+  for (auto [a, n] : {std::pair{&sl.x, K * 3 * nt}, std::pair{&sl.v, K * 3 * nt},
+                      std::pair{&sl.fint, K * 3 * nt}, std::pair{&sl.nrm, K * 3 * et},
+                      std::pair{&sl.ramp, K * 6 * nbt}, std::pair{&sl.sigma, K * 6 * R},
+                      std::pair{&sl.res, K * R}, std::pair{&sl.F, K * 9}})
+    if (e == cudaSuccess) e = a->alloc(n);
+  for (auto [a, n] : {std::pair{&sl.status, K * R}, std::pair{&sl.steps, K * R},
+                      std::pair{&sl.queue, K}})
+    if (e == cudaSuccess) e = a->alloc(n);
+  for (size_t k = 0; k < K && e == cudaSuccess; ++k) {
+    e = cudaStreamCreateWithFlags(&sl.st[k], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.join[k], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.fork, cudaEventDisableTiming);
+  if (e == cudaSuccess && b->precision == MFG_PREC_MIXED)
+    e = mfg::mixed_prepare_contexts(*b->mixed, b->dev, kStiffSlots);
+  if (e != cudaSuccess) {
+    sl.release();
+    return fail(e == cudaErrorMemoryAllocation ? MFG_E_OOM : MFG_E_CUDA,
+                "concurrent stiffness scratch: %s", cudaGetErrorString(e));
+  }
+  sl.ready = true;
+  return MFG_OK;
+}
+
+// The six perturbed, non-updating solves in flight at once, one slot of
+// scratch each, all starting from the state of the last updating run; the
+// batch's current coordinates end as the sixth solve leaves them, as after
+// the reference's six sequential runs. sigma1 receives 6 x n_rve x 6.
+mfg_status stiffness_concurrent(mfg_batch* b, const double Fa[kStiffSlots][9], double* sigma1,
+                                mfg_status* worst) {
+  mfg_status st = stiff_slots_ready(b);
+  if (st != MFG_OK) return st;
+  StiffSlots& sl = b->stiff;
+  cudaStream_t s = b->stream;
+  const int64_t nt = b->nt, et = b->et, R = b->R, nbt = std::max<int64_t>(b->nbt, 1);
+  b->timing_valid = false;
+  MFG_CUDA(cudaEventRecord(b->ev_run0, s));
+  MFG_CUDA(cudaMemcpyAsync(sl.F.p, Fa, sizeof(double) * 9 * kStiffSlots, cudaMemcpyHostToDevice, s));
+  for (int k = 0; k < kStiffSlots; ++k)
+    MFG_CUDA(cudaMemcpyAsync(sl.x.p + 3 * nt * k, b->d_x.p, 3 * nt * sizeof(double),
+                             cudaMemcpyDeviceToDevice, s));
+  MFG_CUDA(cudaEventRecord(b->ev_relax0, s));
+  MFG_CUDA(cudaEventRecord(sl.fork, s));
+  int launches = 0;
+  const int grid = std::min(b->R, b->sms * mfg::relax_f64_max_blocks_per_sm(0));
+  for (int k = 0; k < kStiffSlots; ++k) {
+    cudaStream_t sk = sl.st[k];
+    MFG_CUDA(cudaStreamWaitEvent(sk, sl.fork, 0));
+    mfg::DevBatch bk = b->dev;
+    bk.x = sl.x.p + 3 * nt * k;
+    bk.v = sl.v.p + 3 * nt * k;
+    bk.fint = sl.fint.p + 3 * nt * k;
+    bk.nrm = sl.nrm.p + 3 * et * k;
+    bk.ramp = sl.ramp.p + 6 * nbt * k;
+    bk.queue = sl.queue.p + k;
+    mfg::RunArgs ak{};
+    ak.F = sl.F.p + 9 * k;
+    ak.n_F = 1;
+    ak.update_coords = 0;
+    ak.sigma = sl.sigma.p + 6 * R * k;
+    ak.st_status = sl.status.p + R * k;
+    ak.st_steps = sl.steps.p + R * k;
+    ak.st_residual = sl.res.p + R * k;
+    cudaError_t e;
+    if (b->precision == MFG_PREC_MIXED) {
+      int n = 0;
+      e = mfg::run_mixed(*b->mixed, bk, ak, sk, &n, k + 1);
+      launches += n;
+    } else {
+      e = cudaMemsetAsync(bk.queue, 0, sizeof(int32_t), sk);
+      if (e == cudaSuccess) e = mfg::launch_relax_f64(bk, ak, 0, grid, sk);
+      launches += 1;
+    }
+    if (e != cudaSuccess)
+      return fail(MFG_E_CUDA, "stiffness solve %d failed to launch: %s", k, cudaGetErrorString(e));
+    MFG_CUDA(cudaEventRecord(sl.join[k], sk));
+    MFG_CUDA(cudaStreamWaitEvent(s, sl.join[k], 0));
+  }
+  MFG_CUDA(cudaEventRecord(b->ev_relax1, s));
+  b->last_launches = launches;
+  MFG_CUDA(cudaMemcpyAsync(b->d_x.p, sl.x.p + 3 * nt * (kStiffSlots - 1), 3 * nt * sizeof(double),
+                           cudaMemcpyDeviceToDevice, s));
+  std::vector<int32_t> hst(static_cast<size_t>(kStiffSlots) * R);
+  MFG_CUDA(cudaMemcpyAsync(sigma1, sl.sigma.p, sizeof(double) * 6 * R * kStiffSlots,
+                           cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(cudaMemcpyAsync(hst.data(), sl.status.p, sizeof(int32_t) * R * kStiffSlots,
+                           cudaMemcpyDeviceToHost, s));
+  MFG_CUDA(cudaEventRecord(b->ev_run1, s));
+  MFG_CUDA(cudaStreamSynchronize(s));
+  b->timing_valid = true;
+  *worst = MFG_OK;
+  for (int32_t v : hst)
+    if (v > *worst) *worst = static_cast<mfg_status>(v);
+  return MFG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 mfg_status mfg_batch_material_stiffness(mfg_batch* b, double* C) {
   mfg::Trace trace("mfg_batch_material_stiffness");
   g_last_error.clear();
   if (!b || !C) return fail(MFG_E_INVALID, "NULL argument");
   MFG_CUDA(cudaSetDevice(b->device));
   // BatchedFiberRVEAnalysisExplicit.h:321-405
-  constexpr double h = 1E-5;
-  double D1 = std::sqrt(1.0 / (1 - 2 * h));
-  constexpr double l1 = 1;
-  constexpr double l2 = (1 + h) / (1 - h * h);
-  constexpr double l3 = (1 - h) / (1 - h * h);
-  double l2pl3 = 0.5 * (std::sqrt(l2) + std::sqrt(l3));
-  double l2ml3 = 0.5 * (std::sqrt(l2) - std::sqrt(l3));
-  std::vector<double> cur(6 * b->R), sigma1(6 * b->R);
+  constexpr double h = kStiffH;
+  double Fa[kStiffSlots][9];
+  perturbation_gradients(Fa);
+  std::vector<double> cur(6 * b->R), sigma1(6 * b->R * static_cast<size_t>(kStiffSlots));
   MFG_CUDA(cudaMemcpy(cur.data(), b->d_cur.p, 6 * sizeof(double) * b->R, cudaMemcpyDeviceToHost));
   mfg_status worst = MFG_OK;
-  for (int i = 0; i < 6; ++i) {
-    double Fa[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    switch (i) {
-      case 0: Fa[0] = D1; Fa[4] = 1; Fa[8] = 1; break;
-      case 1: Fa[0] = 1; Fa[4] = D1; Fa[8] = 1; break;
-      case 2: Fa[0] = 1; Fa[4] = 1; Fa[8] = D1; break;
-      case 3: Fa[0] = l1; Fa[4] = l2pl3; Fa[8] = l2pl3; Fa[5] = l2ml3; Fa[7] = l2ml3; break;
-      case 4: Fa[0] = l2pl3; Fa[4] = l1; Fa[8] = l2pl3; Fa[2] = l2ml3; Fa[6] = l2ml3; break;
-      default: Fa[0] = l2pl3; Fa[4] = l2pl3; Fa[8] = l1; Fa[1] = l2ml3; Fa[3] = l2ml3; break;
+  const bool concurrent = b->stiffness == MFG_STIFFNESS_CONCURRENT ||
+                          (b->stiffness == MFG_STIFFNESS_AUTO && b->all_ramp);
+  if (concurrent) {
+    mfg_status st = stiffness_concurrent(b, Fa, sigma1.data(), &worst);
+    if (st != MFG_OK) return st;
+  } else {
+    for (int i = 0; i < kStiffSlots; ++i) {
+      mfg_status st = mfg_batch_run(b, Fa[i], 1, sigma1.data() + 6 * b->R * i, 0, nullptr);
+      if (st == MFG_E_INVALID || st == MFG_E_CUDA || st == MFG_E_OOM) return st;
+      if (st > worst) worst = st;
     }
-    mfg_status st = mfg_batch_run(b, Fa, 1, sigma1.data(), 0, nullptr);
-    if (st == MFG_E_INVALID || st == MFG_E_CUDA || st == MFG_E_OOM) return st;
-    if (st > worst) worst = st;
-    for (int r = 0; r < b->R; ++r)
-      for (int j = 0; j < 6; ++j) C[36 * r + 6 * j + i] = (sigma1[6 * r + j] - cur[6 * r + j]) / h;
   }
+  for (int i = 0; i < kStiffSlots; ++i)
+    for (int r = 0; r < b->R; ++r)
+      for (int j = 0; j < 6; ++j)
+        C[36 * r + 6 * j + i] = (sigma1[6 * b->R * i + 6 * r + j] - cur[6 * r + j]) / h;
+  if (worst != MFG_OK)
+    fail(worst, "%s in at least one perturbed solve", mfg_status_string(worst));
   return worst;
 }
 
@@ -902,7 +1073,7 @@ double now_s() {
 
 struct PendingReq {
   int64_t ticket;
-  int32_t update;
+  int32_t flags;  // mfg::kReqUpdate | mfg::kReqStiffness
   double F[9];
   double t_submit;
 };
@@ -965,6 +1136,9 @@ struct mfg_server {
   int* ctl_d = nullptr;  // [0] idle CTAs (or clusters), [1] closing
   DevArray<double> sigma, res;
   DevArray<int32_t> st, steps;
+  // stiffness of a request: perturbation gradients, perturbed-solve scratch, result
+  DevArray<double> stiff_F, sigma1, res1, C;
+  DevArray<int32_t> st1, steps1, stiff_status;
   int64_t next_ticket = 0;
   int64_t launches = 0;
   std::vector<uint8_t> busy;
@@ -995,10 +1169,8 @@ struct mfg_server {
     if (stop_d) cudaFree(stop_d);
     if (last_d) cudaFree(last_d);
     if (ctl_d) cudaFree(ctl_d);
-    sigma.release();
-    res.release();
-    st.release();
-    steps.release();
+    for (auto* a : {&sigma, &res, &stiff_F, &sigma1, &res1, &C}) a->release();
+    for (auto* a : {&st, &steps, &st1, &steps1, &stiff_status}) a->release();
     mfg_batch_destroy(batch);
   }
 };
@@ -1035,7 +1207,7 @@ mfg_status server_publish(mfg_server* sv, int32_t rve, const PendingReq& p) {
   const int64_t idx = l.tail;
   mfg::ServerReq& q = l.ring_h[idx % sv->cap];
   q.rve = rve;
-  q.update_coords = p.update;
+  q.flags = p.flags;
   q.ticket = p.ticket;
   for (int k = 0; k < 9; ++k) q.F[k] = p.F[k];
   l.slot_ticket[idx % sv->cap] = p.ticket;
@@ -1079,6 +1251,14 @@ mfg_status server_lane_create(mfg_server* sv, ServerLane& l) {
   a.st_status = sv->st.p;
   a.st_steps = sv->steps.p;
   a.st_residual = sv->res.p;
+  a.stiff_F = sv->stiff_F.p;
+  a.cur_stress = sv->batch->d_cur.p;
+  a.sigma1 = sv->sigma1.p;
+  a.st1_status = sv->st1.p;
+  a.st1_steps = sv->steps1.p;
+  a.st1_residual = sv->res1.p;
+  a.C = sv->C.p;
+  a.stiff_status = sv->stiff_status.p;
   l.slot_ticket.assign(sv->cap, -1);
   l.slot_submit.assign(sv->cap, 0.0);
   l.slot_returned.assign(sv->cap, 1);
@@ -1154,6 +1334,18 @@ mfg_status mfg_server_create(const mfg_network* nets, const mfg_strategy* strate
   MFG_CUDA(sv->res.alloc(n_rve));
   MFG_CUDA(sv->st.alloc(n_rve));
   MFG_CUDA(sv->steps.alloc(n_rve));
+  {
+    double Fa[kStiffSlots][9];
+    perturbation_gradients(Fa);
+    MFG_CUDA(sv->stiff_F.alloc(9 * kStiffSlots));
+    MFG_CUDA(cudaMemcpy(sv->stiff_F.p, Fa, sizeof(Fa), cudaMemcpyHostToDevice));
+  }
+  MFG_CUDA(sv->sigma1.alloc(6 * static_cast<size_t>(n_rve)));
+  MFG_CUDA(sv->res1.alloc(n_rve));
+  MFG_CUDA(sv->C.alloc(36 * static_cast<size_t>(n_rve)));
+  MFG_CUDA(sv->st1.alloc(n_rve));
+  MFG_CUDA(sv->steps1.alloc(n_rve));
+  MFG_CUDA(sv->stiff_status.alloc(n_rve));
   // RVEs the mixed serving kernel solves with clusters get their own ring
   sv->lane_of.assign(n_rve, 0);
   bool clusters = false;
@@ -1175,6 +1367,11 @@ mfg_status mfg_server_create(const mfg_network* nets, const mfg_strategy* strate
 
 mfg_status mfg_server_submit(mfg_server* sv, int32_t rve, const double* F, int32_t update_coords,
                              int64_t* ticket) {
+  return mfg_server_submit_ex(sv, rve, F, update_coords, 0, ticket);
+}
+
+mfg_status mfg_server_submit_ex(mfg_server* sv, int32_t rve, const double* F,
+                                int32_t update_coords, int32_t stiffness, int64_t* ticket) {
   g_last_error.clear();
   if (!sv || !F) return fail(MFG_E_INVALID, "NULL argument");
   if (rve < 0 || rve >= sv->batch->R) return fail(MFG_E_INVALID, "rve %d out of range", rve);
@@ -1185,7 +1382,7 @@ mfg_status mfg_server_submit(mfg_server* sv, int32_t rve, const double* F, int32
   MFG_CUDA(cudaSetDevice(sv->batch->device));
   PendingReq p;
   p.ticket = sv->next_ticket++;
-  p.update = update_coords ? 1 : 0;
+  p.flags = (update_coords ? mfg::kReqUpdate : 0) | (stiffness ? mfg::kReqStiffness : 0);
   for (int k = 0; k < 9; ++k) p.F[k] = F[k];
   p.t_submit = now_s();
   if (ticket) *ticket = p.ticket;
@@ -1221,9 +1418,10 @@ mfg_status mfg_server_poll(mfg_server* sv, mfg_server_result* out, int32_t capac
         r.rve = d.rve;
         r.status = d.status;
         r.steps = d.steps;
-        r.pad_ = 0;
+        r.stiffness_status = d.stiff_status;
         r.residual = d.residual;
         for (int k = 0; k < 6; ++k) r.sigma[k] = d.sigma[k];
+        for (int k = 0; k < 36; ++k) r.C[k] = d.stiff_status >= 0 ? d.C[k] : 0.0;
         r.latency_s = now_s() - l.slot_submit[slot];
         r.device_s = 1e-9 * static_cast<double>(d.t_done_ns - d.t_claim_ns);
         r.t_claim_ns = d.t_claim_ns;

@@ -82,19 +82,24 @@ struct RunArgs {
 };
 
 // Serving: request ring and completion records in host-mapped memory.
+constexpr int kReqUpdate = 1;     // ServerReq.flags: update the RVE's state
+constexpr int kReqStiffness = 2;  // ServerReq.flags: also return the material stiffness
+constexpr double kStiffStep = 1E-5;  // FD step of the stiffness (BatchedFiberRVEAnalysisExplicit.h:334)
 struct ServerReq {
   int rve;
-  int update_coords;
+  int flags;  // kReqUpdate | kReqStiffness
   long long ticket;
   double F[9];
   double pad[1];
 };
 struct ServerDone {
   long long ticket_plus1;  // written last: ticket + 1 once the record is valid
-  int rve, status, steps, pad;
+  int rve, status, steps;
+  int stiff_status;  // worst status of the six perturbed solves; -1: no stiffness requested
   double residual;
   double sigma[6];
   long long t_claim_ns, t_done_ns;  // device %globaltimer
+  double C[36];  // material stiffness C[6 j + i], when requested
 };
 struct ServerArgs {
   const ServerReq* ring;            // host-mapped, cap entries
@@ -112,6 +117,16 @@ struct ServerArgs {
   int32_t* st_status;
   int32_t* st_steps;
   double* st_residual;
+  // material stiffness of a request (kReqStiffness): the six perturbation
+  // gradients, per-RVE scratch of the perturbed solves and the result
+  const double* stiff_F;            // device, 6 x 9
+  const double* cur_stress;         // the batch's stress of the last updating run, n_rve * 6
+  double* sigma1;                   // n_rve * 6
+  int32_t* st1_status;              // n_rve
+  int32_t* st1_steps;
+  double* st1_residual;
+  double* C;                        // n_rve * 36
+  int32_t* stiff_status;            // n_rve
 };
 cudaError_t launch_server_f64(const DevBatch& b, const ServerArgs& sa, int grid, cudaStream_t s);
 

@@ -14,6 +14,11 @@ namespace mfg {
 struct MixedState;
 MixedState* mixed_new();
 
+// Run contexts of a mixed batch: 0 for its runs, 1..kMixedContexts-1 for
+// runs in flight at the same time on the same batch (the concurrent
+// perturbed solves of the material stiffness).
+constexpr int kMixedContexts = 7;
+
 // Allocates the mixed-precision working set of a batch and places its RVEs
 // in size buckets. conn, rowptr and inc are the batch's packed fiber ends
 // and CSR rows on the host (RVEs with an order of their own, and the
@@ -25,9 +30,13 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
                          const std::vector<int32_t>& inc, int sms, int max_cluster,
                          bool serving_layout, cudaStream_t s);
 // One run: reads the persistent FP64 state (x, u, vol), relaxes in mixed
-// precision and writes the FP64 state, stress and status back.
+// precision and writes the FP64 state, stress and status back. `ctx` picks
+// the run context (0 for the batch's runs); runs on different contexts may
+// be in flight together when their batch views write disjoint state.
 cudaError_t run_mixed(MixedState& ms, const DevBatch& b, const RunArgs& a, cudaStream_t s,
-                      int* launches);
+                      int* launches, int ctx = 0);
+// Creates run contexts 1..n (n < kMixedContexts) if they do not exist yet.
+cudaError_t mixed_prepare_contexts(MixedState& ms, const DevBatch& b, int n);
 void mixed_destroy(MixedState* ms);
 // Persistent serving kernel on the mixed-precision solve. Without `big`, one
 // CTA per SM serves the `small` ring; with it, 4-CTA clusters serve the

@@ -56,6 +56,28 @@ namespace cg = cooperative_groups;
 
 namespace mfg {
 
+// One run context of a mixed batch: the per-bucket claim counters, the
+// streams and events a run forks over, the captured graph of its last
+// arguments, and the run-time placement's global scratch. Context 0 serves
+// the batch's runs; contexts 1-6 the concurrent perturbed solves of the
+// material stiffness, which run at the same time on the same batch.
+constexpr int kMixedBuckets = 6;
+struct MixedRunCtx {
+  int32_t* queues = nullptr;  // one claim counter per bucket (device)
+  float* u_hl = nullptr;      // run-time placement scratch; null: the batch's own
+  float* v = nullptr;
+  float4* nrm = nullptr;
+  cudaStream_t side[kMixedBuckets] = {};
+  cudaEvent_t fork = nullptr;
+  cudaEvent_t join[kMixedBuckets] = {};
+  cudaStream_t capture = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  RunArgs graph_args{};
+  const double* graph_x = nullptr;  // the batch view's coordinates the graph was captured for
+  int graph_launches = 0;
+  bool ready = false;
+};
+
 struct MixedState {
   float* u_hl = nullptr;   // 6 * nt, node records (hi x, y, z, lo x, y, z); run-time placement
   float* v = nullptr;      // 3 * nt, velocity (x, y, z per node); run-time placement
@@ -95,19 +117,13 @@ struct MixedState {
   // RVEs of bucket q, most fibers first, are order[bucket_off[q] ..
   // bucket_off[q + 1]).
   int32_t* order = nullptr;
-  int32_t* queues = nullptr;  // one claim counter per bucket
   int bucket_off[7] = {};
   int bucket_grid[6] = {};
-  cudaStream_t side[6] = {};
-  cudaEvent_t fork = nullptr;
-  cudaEvent_t join[6] = {};
-  // The batch run as a CUDA graph (queue reset, fork, one launch per bucket,
-  // join), captured for the last run arguments and replayed while they stay
+  // Run contexts (host memory; kernels never touch this pointer). A run is a
+  // CUDA graph (queue reset, fork, one launch per bucket, join), captured
+  // per context for the last run arguments and replayed while they stay
   // the same.
-  cudaStream_t capture = nullptr;
-  cudaGraphExec_t graph = nullptr;
-  RunArgs graph_args{};
-  int graph_launches = 0;
+  MixedRunCtx* ctx = nullptr;
 };
 
 namespace {
@@ -120,7 +136,7 @@ struct BucketKind {
   bool all;    // fiber-centric: force vectors in shared memory too
   bool nodal;  // node-centric solve (node state in shared memory)
 };
-constexpr int kBuckets = 6;
+constexpr int kBuckets = kMixedBuckets;
 constexpr BucketKind kBucket[kBuckets] = {{8, false, true}, {4, false, true}, {2, false, true},
                                           {1, false, true}, {1, true, false}, {1, false, false}};
 // Placement preference (bucket_of): the first bucket whose shared memory
@@ -1135,6 +1151,7 @@ server_cluster_kernel(const DevBatch b, const MixedState ms, const ServerArgs bi
   __shared__ int s_req[2];
   __shared__ int s_mode;
   __shared__ RunArgs s_args;  // read by the solves where needed, not held in registers
+  __shared__ RunArgs s_args1;  // the perturbed solves of a request's stiffness
   cg::cluster_group cl = cg::this_cluster();
   const int rank = static_cast<int>(cl.block_rank());
   const int tid = threadIdx.x;
@@ -1199,12 +1216,26 @@ server_cluster_kernel(const DevBatch b, const MixedState ms, const ServerArgs bi
     if (mode == kServeBig) {
       const long long idx = s_idx;
       const int rve = s_req[0];
+      const int flags = s_req[1];
       const unsigned long long t_claim = global_ns();
-      if (tid == 0) s_args.update_coords = s_req[1];
+      if (tid == 0) s_args.update_coords = flags & kReqUpdate;
       __syncthreads();
-      solve_rve_nodal<kClusterServe>(b, ms, s_args, rve, red, cred,
-                                     smem);  // ends with a cluster barrier
-      if (rank == 0 && tid == 0) server_publish_done(big, idx, rve, t_claim);
+      // the request's solve, then with kReqStiffness the six perturbed
+      // solves of its stiffness, by the cluster
+      const bool stiff = (flags & kReqStiffness) != 0;
+      for (int k = 0; k <= (stiff ? 6 : 0); ++k) {
+        if (k > 0) {
+          if (tid == 0) s_args1 = stiffness_args(big, k - 1);
+          __syncthreads();
+        }
+        solve_rve_nodal<kClusterServe>(b, ms, k == 0 ? s_args : s_args1, rve, red, cred,
+                                       smem);  // ends with a cluster barrier
+        if (k > 0) {
+          if (rank == 0) stiffness_column(big, rve, k - 1);
+          __syncthreads();
+        }
+      }
+      if (rank == 0 && tid == 0) server_publish_done(big, idx, rve, t_claim, stiff);
       cl.sync();
       continue;
     }
@@ -1216,19 +1247,31 @@ server_cluster_kernel(const DevBatch b, const MixedState ms, const ServerArgs bi
           idx = server_try_claim(small);
         if (idx >= 0) {
           server_read_request(small, idx, s_req, s_F);
-          s_args.update_coords = s_req[1];
+          s_args.update_coords = s_req[1] & kReqUpdate;
         }
         s_idx = idx;
       }
       __syncthreads();
       const long long idx = s_idx;
       const int rve = s_req[0];
+      const int flags = s_req[1];
       __syncthreads();
       if (idx < 0) break;
       const unsigned long long t_claim = global_ns();
-      serve_one_cta(b, ms, s_args, rve, red, cred, smem,
-                    smem_floats);  // ends with __syncthreads()
-      if (tid == 0) server_publish_done(small, idx, rve, t_claim);
+      const bool stiff = (flags & kReqStiffness) != 0;
+      for (int j = 0; j <= (stiff ? 6 : 0); ++j) {
+        if (j > 0) {
+          if (tid == 0) s_args1 = stiffness_args(small, j - 1);
+          __syncthreads();
+        }
+        serve_one_cta(b, ms, j == 0 ? s_args : s_args1, rve, red, cred, smem,
+                      smem_floats);  // ends with __syncthreads()
+        if (j > 0) {
+          stiffness_column(small, rve, j - 1);
+          __syncthreads();
+        }
+      }
+      if (tid == 0) server_publish_done(small, idx, rve, t_claim, stiff);
       __syncthreads();
     }
     cl.sync();
@@ -1244,8 +1287,59 @@ cudaError_t alloc(T** p, size_t n) {
 
 MixedState* mixed_new() { return new MixedState(); }
 
+namespace {
+
+void ctx_release(MixedRunCtx& c) {
+  for (void* p : {static_cast<void*>(c.queues), static_cast<void*>(c.u_hl),
+                  static_cast<void*>(c.v), static_cast<void*>(c.nrm)})
+    if (p) cudaFree(p);
+  if (c.graph) cudaGraphExecDestroy(c.graph);
+  if (c.capture) cudaStreamDestroy(c.capture);
+  for (int q = 0; q < kBuckets; ++q) {
+    if (c.side[q]) cudaStreamDestroy(c.side[q]);
+    if (c.join[q]) cudaEventDestroy(c.join[q]);
+  }
+  if (c.fork) cudaEventDestroy(c.fork);
+  c = MixedRunCtx{};
+}
+
+// Creates run context `c` (claim counters, streams, events); with
+// own_scratch, also its own run-time placement scratch, sized like the
+// batch's.
+cudaError_t ctx_init(MixedRunCtx& c, size_t nt, size_t et, bool own_scratch) {
+  cudaError_t e;
+  if ((e = cudaMalloc(reinterpret_cast<void**>(&c.queues), kBuckets * sizeof(int32_t))) !=
+      cudaSuccess)
+    return e;
+  if (own_scratch) {
+    if ((e = cudaMalloc(reinterpret_cast<void**>(&c.u_hl), 6 * std::max<size_t>(nt, 1) *
+                                                              sizeof(float))) != cudaSuccess ||
+        (e = cudaMalloc(reinterpret_cast<void**>(&c.v), 3 * std::max<size_t>(nt, 1) *
+                                                           sizeof(float))) != cudaSuccess ||
+        (e = cudaMalloc(reinterpret_cast<void**>(&c.nrm), std::max<size_t>(et, 1) *
+                                                             sizeof(float4))) != cudaSuccess)
+      return e;
+  }
+  for (int q = 0; q < kBuckets; ++q) {
+    if ((e = cudaStreamCreateWithFlags(&c.side[q], cudaStreamNonBlocking)) != cudaSuccess)
+      return e;
+    if ((e = cudaEventCreateWithFlags(&c.join[q], cudaEventDisableTiming)) != cudaSuccess)
+      return e;
+  }
+  if ((e = cudaEventCreateWithFlags(&c.fork, cudaEventDisableTiming)) != cudaSuccess) return e;
+  if ((e = cudaStreamCreateWithFlags(&c.capture, cudaStreamNonBlocking)) != cudaSuccess) return e;
+  c.ready = true;
+  return cudaSuccess;
+}
+
+}  // namespace
+
 void mixed_destroy(MixedState* ms) {
   if (!ms) return;
+  if (ms->ctx) {
+    for (int k = 0; k < kMixedContexts; ++k) ctx_release(ms->ctx[k]);
+    delete[] ms->ctx;
+  }
   for (void* p : {static_cast<void*>(ms->u_hl), static_cast<void*>(ms->econn),
                   static_cast<void*>(ms->icode), static_cast<void*>(ms->mslot),
                   static_cast<void*>(ms->gnode), static_cast<void*>(ms->mrowptr),
@@ -1255,17 +1349,9 @@ void mixed_destroy(MixedState* ms) {
                   static_cast<void*>(ms->fconc),
                   static_cast<void*>(ms->v), static_cast<void*>(ms->mass),
                   static_cast<void*>(ms->fcon), static_cast<void*>(ms->nrm),
-                  static_cast<void*>(ms->order), static_cast<void*>(ms->queues),
-                  static_cast<void*>(ms->rve_bucket)})
+                  static_cast<void*>(ms->order), static_cast<void*>(ms->rve_bucket)})
     if (p) cudaFree(p);
   delete[] ms->h_cl;
-  if (ms->graph) cudaGraphExecDestroy(ms->graph);
-  if (ms->capture) cudaStreamDestroy(ms->capture);
-  for (int q = 0; q < kBuckets; ++q) {
-    if (ms->side[q]) cudaStreamDestroy(ms->side[q]);
-    if (ms->join[q]) cudaEventDestroy(ms->join[q]);
-  }
-  if (ms->fork) cudaEventDestroy(ms->fork);
   delete ms;
 }
 
@@ -1307,15 +1393,14 @@ cudaLaunchConfig_t launch_config(const MixedState& ms, unsigned grid, cudaStream
 
 template <int CL, bool kAll, bool kNodal>
 cudaError_t launch_bucket(const MixedState& ms, const DevBatch& b, const RunArgs& a, int q,
-                          cudaStream_t s) {
+                          int32_t* queue, cudaStream_t s) {
   const int n = ms.bucket_off[q + 1] - ms.bucket_off[q];
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg =
       launch_config<CL, kAll>(ms, static_cast<unsigned>(ms.bucket_grid[q]), s, attr);
   return cudaLaunchKernelEx(&cfg, relax_mixed_kernel<CL, kAll, kNodal>, b, ms, a,
                             static_cast<int>(ms.smem_bytes / sizeof(float)),
-                            static_cast<const int32_t*>(ms.order + ms.bucket_off[q]), n,
-                            ms.queues + q);
+                            static_cast<const int32_t*>(ms.order + ms.bucket_off[q]), n, queue);
 }
 
 template <int CL, bool kAll, bool kNodal>
@@ -1361,7 +1446,8 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
   if ((e = alloc(&ms.mrowptr, rowptr.size())) != cudaSuccess) return e;
   if ((e = alloc(&ms.mmass, nt)) != cudaSuccess) return e;
   if ((e = alloc(&ms.order, desc.size())) != cudaSuccess) return e;
-  if ((e = alloc(&ms.queues, kBuckets)) != cudaSuccess) return e;
+  ms.ctx = new MixedRunCtx[kMixedContexts];
+  if ((e = ctx_init(ms.ctx[0], nt, et, false)) != cudaSuccess) return e;
   ms.sms = sms;
   ms.smem_bytes = kSmemBytesMixed;
   const int smem_floats = kSmemBytesMixed / static_cast<int>(sizeof(float));
@@ -1507,13 +1593,7 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
         break;
     }
     if (e != cudaSuccess) return e;
-    if ((e = cudaStreamCreateWithFlags(&ms.side[q], cudaStreamNonBlocking)) != cudaSuccess)
-      return e;
-    if ((e = cudaEventCreateWithFlags(&ms.join[q], cudaEventDisableTiming)) != cudaSuccess)
-      return e;
   }
-  if ((e = cudaEventCreateWithFlags(&ms.fork, cudaEventDisableTiming)) != cudaSuccess) return e;
-  if ((e = cudaStreamCreateWithFlags(&ms.capture, cudaStreamNonBlocking)) != cudaSuccess) return e;
 
   const int64_t n = std::max<int64_t>(b.nt, 1);
   mixed_prepare_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(b, ms);
@@ -1560,44 +1640,45 @@ cudaError_t launch_server_mixed(MixedState& ms, const DevBatch& b, const ServerA
 
 namespace {
 
-// One launch per non-empty size bucket, each on its own stream so that the
-// buckets run concurrently: the largest clusters are launched first, and the
-// CTAs of the later buckets take over SMs as the earlier buckets drain.
-cudaError_t enqueue_buckets(MixedState& ms, const DevBatch& b, const RunArgs& a, cudaStream_t s,
-                            int* launches) {
+// One launch per non-empty size bucket, each on its own stream of context
+// `c` so that the buckets run concurrently: the largest clusters are
+// launched first, and the CTAs of the later buckets take over SMs as the
+// earlier buckets drain.
+cudaError_t enqueue_buckets(const MixedState& ms, MixedRunCtx& c, const DevBatch& b,
+                            const RunArgs& a, cudaStream_t s, int* launches) {
   cudaError_t e;
   *launches = 0;
-  if ((e = cudaMemsetAsync(ms.queues, 0, kBuckets * sizeof(int32_t), s)) != cudaSuccess)
-    return e;
-  if ((e = cudaEventRecord(ms.fork, s)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(c.queues, 0, kBuckets * sizeof(int32_t), s)) != cudaSuccess) return e;
+  if ((e = cudaEventRecord(c.fork, s)) != cudaSuccess) return e;
   for (int q = 0; q < kBuckets; ++q) {
     if (ms.bucket_off[q + 1] == ms.bucket_off[q]) continue;
-    cudaStream_t sq = ms.side[q];
-    if ((e = cudaStreamWaitEvent(sq, ms.fork, 0)) != cudaSuccess) return e;
+    cudaStream_t sq = c.side[q];
+    if ((e = cudaStreamWaitEvent(sq, c.fork, 0)) != cudaSuccess) return e;
+    int32_t* queue = c.queues + q;
     switch (q) {
       case 0:
-        e = launch_bucket<kBucket[0].cl, kBucket[0].all, kBucket[0].nodal>(ms, b, a, q, sq);
+        e = launch_bucket<kBucket[0].cl, kBucket[0].all, kBucket[0].nodal>(ms, b, a, q, queue, sq);
         break;
       case 1:
-        e = launch_bucket<kBucket[1].cl, kBucket[1].all, kBucket[1].nodal>(ms, b, a, q, sq);
+        e = launch_bucket<kBucket[1].cl, kBucket[1].all, kBucket[1].nodal>(ms, b, a, q, queue, sq);
         break;
       case 2:
-        e = launch_bucket<kBucket[2].cl, kBucket[2].all, kBucket[2].nodal>(ms, b, a, q, sq);
+        e = launch_bucket<kBucket[2].cl, kBucket[2].all, kBucket[2].nodal>(ms, b, a, q, queue, sq);
         break;
       case 3:
-        e = launch_bucket<kBucket[3].cl, kBucket[3].all, kBucket[3].nodal>(ms, b, a, q, sq);
+        e = launch_bucket<kBucket[3].cl, kBucket[3].all, kBucket[3].nodal>(ms, b, a, q, queue, sq);
         break;
       case 4:
-        e = launch_bucket<kBucket[4].cl, kBucket[4].all, kBucket[4].nodal>(ms, b, a, q, sq);
+        e = launch_bucket<kBucket[4].cl, kBucket[4].all, kBucket[4].nodal>(ms, b, a, q, queue, sq);
         break;
       default:
-        e = launch_bucket<kBucket[5].cl, kBucket[5].all, kBucket[5].nodal>(ms, b, a, q, sq);
+        e = launch_bucket<kBucket[5].cl, kBucket[5].all, kBucket[5].nodal>(ms, b, a, q, queue, sq);
         break;
     }
     if (e != cudaSuccess) return e;
     ++*launches;
-    if ((e = cudaEventRecord(ms.join[q], sq)) != cudaSuccess) return e;
-    if ((e = cudaStreamWaitEvent(s, ms.join[q], 0)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(c.join[q], sq)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(s, c.join[q], 0)) != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
@@ -1610,20 +1691,45 @@ bool same_args(const RunArgs& x, const RunArgs& y) {
 
 }  // namespace
 
-// A run replays the captured graph when the arguments (device pointers and
-// flags) are those it was captured with; otherwise the bucket launches are
-// captured on a private stream into a new graph first.
+cudaError_t mixed_prepare_contexts(MixedState& ms, const DevBatch& b, int n) {
+  if (n >= kMixedContexts) return cudaErrorInvalidValue;
+  // the run-time placement keeps node records, velocities and force vectors
+  // in global memory: concurrent runs need their own
+  const bool runtime_bucket = ms.bucket_off[kBuckets] > ms.bucket_off[kBuckets - 1];
+  for (int k = 1; k <= n; ++k) {
+    if (ms.ctx[k].ready) continue;
+    cudaError_t e = ctx_init(ms.ctx[k], static_cast<size_t>(b.nt), static_cast<size_t>(b.et),
+                             runtime_bucket);
+    if (e != cudaSuccess) {
+      ctx_release(ms.ctx[k]);
+      return e;
+    }
+  }
+  return cudaSuccess;
+}
+
+// A run replays context k's captured graph when the arguments (the batch
+// view's coordinates, device pointers and flags) are those it was captured
+// with; otherwise the bucket launches are captured on the context's private
+// stream into a new graph first.
 cudaError_t run_mixed(MixedState& ms, const DevBatch& b, const RunArgs& a, cudaStream_t s,
-                      int* launches) {
+                      int* launches, int k) {
+  if (k < 0 || k >= kMixedContexts || !ms.ctx[k].ready) return cudaErrorInvalidValue;
+  MixedRunCtx& c = ms.ctx[k];
   cudaError_t e;
-  if (!ms.graph || !same_args(ms.graph_args, a)) {
-    if ((e = cudaStreamBeginCapture(ms.capture, cudaStreamCaptureModeThreadLocal)) !=
-        cudaSuccess)
+  if (!c.graph || !same_args(c.graph_args, a) || c.graph_x != b.x) {
+    MixedState msc = ms;  // the kernels' view: this context's run-time scratch
+    if (c.u_hl) {
+      msc.u_hl = c.u_hl;
+      msc.v = c.v;
+      msc.nrm = c.nrm;
+    }
+    if ((e = cudaStreamBeginCapture(c.capture, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
       return e;
     int n = 0;
-    const cudaError_t ec = enqueue_buckets(ms, b, a, ms.capture, &n);
+    const cudaError_t ec = enqueue_buckets(msc, c, b, a, c.capture, &n);
     cudaGraph_t g = nullptr;
-    e = cudaStreamEndCapture(ms.capture, &g);
+    e = cudaStreamEndCapture(c.capture, &g);
     if (ec != cudaSuccess || e != cudaSuccess) {
       if (g) cudaGraphDestroy(g);
       return ec != cudaSuccess ? ec : e;
@@ -1632,13 +1738,14 @@ cudaError_t run_mixed(MixedState& ms, const DevBatch& b, const RunArgs& a, cudaS
     e = cudaGraphInstantiate(&exec, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return e;
-    if (ms.graph) cudaGraphExecDestroy(ms.graph);
-    ms.graph = exec;
-    ms.graph_args = a;
-    ms.graph_launches = n;
+    if (c.graph) cudaGraphExecDestroy(c.graph);
+    c.graph = exec;
+    c.graph_args = a;
+    c.graph_x = b.x;
+    c.graph_launches = n;
   }
-  *launches = ms.graph_launches;
-  return cudaGraphLaunch(ms.graph, s);
+  *launches = c.graph_launches;
+  return cudaGraphLaunch(c.graph, s);
 }
 
 }  // namespace mfg

@@ -28,6 +28,9 @@ def _lib():
                                         i32, C.POINTER(_abi.mfg_server_options), C.POINTER(vp)]
         L.mfg_server_submit.restype = i32
         L.mfg_server_submit.argtypes = [vp, i32, C.POINTER(C.c_double), i32, C.POINTER(i64)]
+        L.mfg_server_submit_ex.restype = i32
+        L.mfg_server_submit_ex.argtypes = [vp, i32, C.POINTER(C.c_double), i32, i32,
+                                           C.POINTER(i64)]
         L.mfg_server_poll.restype = i32
         L.mfg_server_poll.argtypes = [vp, vp, i32, C.POINTER(i32), i32]
         L.mfg_server_outstanding.restype = i64
@@ -84,11 +87,14 @@ class RVEServer:
     def __exit__(self, *exc):
         self.close()
 
-    def submit(self, rve: int, F, update_coords: bool = True) -> int:
+    def submit(self, rve: int, F, update_coords: bool = True, stiffness: bool = False) -> int:
+        """Queues one solve; with stiffness=True the result also carries the
+        RVE's material stiffness (field C, (6, 6), as computeMaterialStiffness
+        returns it), from six perturbed solves run right after this one."""
         Fv = np.ascontiguousarray(np.asarray(F, dtype=np.float64).reshape(9))
         t = C.c_int64()
-        _check(_lib().mfg_server_submit(self._h, int(rve), dptr(Fv), int(bool(update_coords)),
-                                        C.byref(t)))
+        _check(_lib().mfg_server_submit_ex(self._h, int(rve), dptr(Fv), int(bool(update_coords)),
+                                           int(bool(stiffness)), C.byref(t)))
         return t.value
 
     def poll(self, max_results: int = 4096, timeout_ms: int = 1000) -> np.ndarray:

@@ -25,13 +25,13 @@ ids give the same networks on x86-64 and aarch64.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass
 from typing import List
 
 import numpy as np
 
-from . import batched
 from ._abi import MFG_MODE_RAMP, dptr
 from .network_io import LINEAR, NONLINEAR, FiberNetwork, Reaction
 from .strategy import SolutionStrategy
@@ -40,9 +40,28 @@ SNAP = 0.02
 MIN_SEP = 1e-6
 
 
+_netgen = None
+_netgen_path = None
+
+
+def use_netgen_library(path: str) -> None:
+    """Takes the network generator from the shared library at `path` (a
+    build of netgen.cpp) instead of mumfim_gb300/_lib/libmumfim_netgen.so;
+    call before the first network is generated."""
+    global _netgen_path
+    if _netgen is not None and path != _netgen_path:
+        raise RuntimeError("the network generator is already loaded")
+    _netgen_path = path
+
+
 def _lib():
-    L = batched.load_library()
-    if not getattr(L, "_netgen_ready", False):
+    global _netgen
+    if _netgen is None:
+        from .build import NETGEN_PATH
+        p = _netgen_path or NETGEN_PATH
+        if not os.path.exists(p):
+            raise ImportError(f"{p} is missing; build it with `python -m mumfim_gb300.build`")
+        L = C.CDLL(p)
         L.mfg_generate_knn_network.restype = C.c_int32
         L.mfg_generate_knn_network.argtypes = [C.c_int32, C.c_int32, C.c_uint64, C.c_double,
                                                C.c_double, C.POINTER(C.c_double),
@@ -53,8 +72,8 @@ def _lib():
         for n in ("mfg_portable_exp", "mfg_portable_log"):
             getattr(L, n).restype = C.c_double
             getattr(L, n).argtypes = [C.c_double]
-        L._netgen_ready = True
-    return L
+        _netgen = L
+    return _netgen
 
 
 def knn_network(n_nodes: int, k: int, seed: int, snap: float = SNAP, min_sep: float = MIN_SEP):

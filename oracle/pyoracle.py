@@ -7,6 +7,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import platform
 import subprocess
 
 import numpy as np
@@ -18,31 +19,65 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
+FAST_LIB_PATH = os.path.join(BUILD_DIR, "liboracle_fast.so")
+NETGEN_PATH = os.path.join(BUILD_DIR, "libnetgen.so")
+
+# Parity build: no contraction and no target-specific code, so x86-64 and
+# aarch64 give the same bits as the FP64 GPU kernel.
+PARITY_FLAGS = ["-O2", "-ffp-contract=off"]
+
+
+def timing_flags() -> list:
+    """Timing build of the same source for the CPU baseline: -O3, loop
+    unrolling, contraction into FMAs allowed, and the GPU machine's host core
+    named explicitly (Neoverse V2 on aarch64). Its results differ from the
+    parity build's in the last bits only (test_oracle_golden checks 1e-9)."""
+    flags = ["-O3", "-funroll-loops", "-ffp-contract=fast"]
+    if platform.machine() in ("aarch64", "arm64"):
+        flags.append("-mcpu=neoverse-v2")
+    return flags
+
+
+def _compile(out: str, flags: list, force: bool) -> str:
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    src = os.path.join(HERE, "mumfim_oracle.cpp")
+    deps = [src, os.path.join(HERE, "mumfim_oracle.h"), __file__]
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= max(
+            os.path.getmtime(d) for d in deps):
+        return out
+    cmd = ["g++", *flags, "-std=c++17", "-fPIC", "-shared", "-pthread",
+           "-I" + os.path.join(REPO, "include"), "-I" + HERE, src, "-o", out + ".tmp"]
+    subprocess.run(cmd, check=True)
+    os.replace(out + ".tmp", out)
+    return out
 
 
 def build(force: bool = False) -> str:
-    """Compiles the oracle (-O2 -ffp-contract=off, no -march so x86-64 and
-    aarch64 give the same bits)."""
-    os.makedirs(BUILD_DIR, exist_ok=True)
-    src = os.path.join(HERE, "mumfim_oracle.cpp")
-    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= max(
-            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "mumfim_oracle.h"))):
-        return LIB_PATH
-    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",
-           "-I" + os.path.join(REPO, "include"), "-I" + HERE, src, "-o", LIB_PATH + ".tmp"]
-    subprocess.run(cmd, check=True)
-    os.replace(LIB_PATH + ".tmp", LIB_PATH)
-    return LIB_PATH
+    """Compiles the oracle's parity build, its timing build and a copy of the
+    network generator for the CPU-only reference arm; returns the parity
+    build's path."""
+    _compile(FAST_LIB_PATH, timing_flags(), force)
+    build_netgen(force)
+    return _compile(LIB_PATH, PARITY_FLAGS, force)
 
 
-_lib = None
+def build_netgen(force: bool = False) -> str:
+    """The synthetic-network generator compiled into oracle/_build, so that
+    the CPU-only reference arm of the benchmark maps no library of the
+    product."""
+    from mumfim_gb300.build import build_netgen as _bn
+    return _bn(NETGEN_PATH, force)
 
 
-def lib():
-    global _lib
-    if _lib is None:
+_libs = {}
+
+
+def lib(timing: bool = False):
+    """The parity build (default) or the timing build, loaded with ctypes."""
+    key = "timing" if timing else "parity"
+    if key not in _libs:
         build()
-        L = C.CDLL(LIB_PATH)
+        L = C.CDLL(FAST_LIB_PATH if timing else LIB_PATH)
         L.orc_batch_create.restype = C.c_void_p
         L.orc_batch_create.argtypes = [C.POINTER(mfg_network), C.POINTER(mfg_strategy), C.c_int32]
         L.orc_batch_destroy.argtypes = [C.c_void_p]
@@ -72,25 +107,28 @@ def lib():
         L.orc_nodal_mass.argtypes = [C.c_int32, C.POINTER(C.c_double), C.c_int32,
                                      C.POINTER(C.c_int32), C.c_double, C.c_double,
                                      C.POINTER(C.c_double)]
-        _lib = L
-    return _lib
+        _libs[key] = L
+    return _libs[key]
 
 
 class OracleBatch:
     """CPU restatement of BatchedFiberRVEAnalysisExplicit with the same
     arguments as mumfim_gb300.BatchedFiberRVEAnalysisExplicit."""
 
-    def __init__(self, networks, strategies):
+    def __init__(self, networks, strategies, timing: bool = False):
+        """timing=True uses the optimised timing build (CPU baseline) instead
+        of the bit-stable parity build."""
+        self._L = lib(timing)
         self._arr = NetworkArray(networks, strategies)
         self.n_rve = len(networks)
         self.n_nodes = [n.n_nodes for n in networks]
-        self._h = lib().orc_batch_create(self._arr.nets, self._arr.strats, self.n_rve)
+        self._h = self._L.orc_batch_create(self._arr.nets, self._arr.strats, self.n_rve)
         if not self._h:
             raise ValueError("oracle rejected the networks")
 
     def close(self):
         if self._h:
-            lib().orc_batch_destroy(self._h)
+            self._L.orc_batch_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -100,39 +138,39 @@ class OracleBatch:
         F = np.ascontiguousarray(F, dtype=np.float64).reshape(-1, 9)
         sigma = np.zeros((self.n_rve, 6))
         st = np.zeros(self.n_rve, dtype=RVE_STATUS_DTYPE)
-        rc = lib().orc_batch_run(self._h, dptr(F), F.shape[0], dptr(sigma), int(update_coords),
+        rc = self._L.orc_batch_run(self._h, dptr(F), F.shape[0], dptr(sigma), int(update_coords),
                                  st.ctypes.data_as(C.c_void_p), n_threads)
         return rc, sigma, st
 
     def material_stiffness(self, n_threads=1):
         Cm = np.zeros((self.n_rve, 6, 6))
-        rc = lib().orc_batch_material_stiffness(self._h, dptr(Cm), n_threads)
+        rc = self._L.orc_batch_material_stiffness(self._h, dptr(Cm), n_threads)
         return rc, Cm
 
     def orientation_3d(self):
         om = np.zeros((self.n_rve, 3, 3))
-        lib().orc_batch_orientation_3d(self._h, dptr(om))
+        self._L.orc_batch_orientation_3d(self._h, dptr(om))
         return om
 
     def orientation_2d(self, normal):
         normal = np.ascontiguousarray(normal, dtype=np.float64).reshape(self.n_rve, 3)
         om = np.zeros((self.n_rve, 3, 3))
-        lib().orc_batch_orientation_2d(self._h, dptr(normal), dptr(om))
+        self._L.orc_batch_orientation_2d(self._h, dptr(normal), dptr(om))
         return om
 
     def displacements(self, rve):
         u = np.zeros((self.n_nodes[rve], 3))
-        lib().orc_batch_get_displacements(self._h, rve, dptr(u))
+        self._L.orc_batch_get_displacements(self._h, rve, dptr(u))
         return u
 
     def coordinates(self, rve):
         x = np.zeros((self.n_nodes[rve], 3))
-        lib().orc_batch_get_coordinates(self._h, rve, dptr(x))
+        self._L.orc_batch_get_coordinates(self._h, rve, dptr(x))
         return x
 
     def current_stress(self):
         s = np.zeros((self.n_rve, 6))
-        lib().orc_batch_get_current_stress(self._h, dptr(s))
+        self._L.orc_batch_get_current_stress(self._h, dptr(s))
         return s
 
 

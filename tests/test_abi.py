@@ -10,23 +10,28 @@ import pytest
 from conftest import REPO
 
 
-def _declared_functions():
-    names = []
-    for h in sorted(os.listdir(os.path.join(REPO, "include"))):
-        if not h.endswith(".h"):
-            continue
-        src = open(os.path.join(REPO, "include", h)).read()
-        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-        names += re.findall(r"^\s*[A-Za-z_][\w\s\*]*?\b(mfg_\w+)\s*\(", src, flags=re.M)
-    return sorted(set(names))
+def _declared_functions(header):
+    src = open(os.path.join(REPO, "include", header)).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*[A-Za-z_][\w\s\*]*?\b(mfg_\w+)\s*\(", src,
+                                 flags=re.M)))
 
 
 def test_library_exports_every_declared_symbol(lib_path):
-    lib = C.CDLL(lib_path)
-    names = _declared_functions()
-    assert len(names) >= 25
-    missing = [n for n in names if not hasattr(lib, n)]
-    assert not missing, missing
+    """mumfim_gpu.h is the solver library's ABI, mumfim_netgen.h the network
+    generator's; every header in include/ belongs to one of them."""
+    from mumfim_gb300.build import NETGEN_PATH
+    owner = {"mumfim_gpu.h": lib_path, "mumfim_netgen.h": NETGEN_PATH}
+    headers = sorted(h for h in os.listdir(os.path.join(REPO, "include")) if h.endswith(".h"))
+    assert headers == sorted(owner)
+    for h, path in owner.items():
+        lib = C.CDLL(path)
+        names = _declared_functions(h)
+        assert len(names) >= (25 if h == "mumfim_gpu.h" else 4)
+        missing = [n for n in names if not hasattr(lib, n)]
+        assert not missing, (h, missing)
+    gpu = C.CDLL(lib_path)
+    assert not hasattr(gpu, "mfg_generate_knn_network")
 
 
 def test_status_strings_and_defaults(lib_path):

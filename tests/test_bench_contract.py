@@ -67,3 +67,21 @@ def test_reference_arm_under_torchrun_prints_once():
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+
+
+def test_reference_arm_maps_no_product_library():
+    """The reference arm generates its workload with the oracle's own build of
+    the network generator and times the oracle: no library of the product is
+    loaded into that process."""
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', "
+            "'--warmup', '3', '--n-rve', '4', '--cpu-sample-rves', '1', '--solve-steps', '50']; "
+            "runpy.run_path('bench.py', run_name='__main__'); "
+            "print('MAPS', sorted({l.split()[-1] for l in open('/proc/self/maps') "
+            "if l.rstrip().endswith('.so')}))")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    maps = [x for x in r.stdout.splitlines() if x.startswith("MAPS")][0]
+    assert "oracle/_build/liboracle_fast.so" in maps
+    assert "oracle/_build/libnetgen.so" in maps
+    assert "mumfim_gb300/_lib" not in maps, maps

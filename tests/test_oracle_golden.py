@@ -111,3 +111,17 @@ def test_transactional_run_restores_displacement(oracle, golden_2_7):
     u0 = b.displacements(0).copy()
     b.run(np.diag([1.01, 1, 1]).reshape(1, 3, 3), update_coords=False)
     np.testing.assert_array_equal(b.displacements(0), u0)
+
+
+def test_timing_build_agrees_with_the_parity_build(oracle):
+    """The CPU baseline times the oracle's optimised build (-O3, FMA
+    contraction allowed); it must solve the same problem: stresses within
+    1e-9 of the bit-stable parity build on a fixed-step case."""
+    from mumfim_gb300 import synthetic as S
+    w = S.config1(n_rve=3, n_nodes=500, steps=500)
+    rc, sig, st = oracle.OracleBatch(w.networks, w.strategies).run(w.F, n_threads=3)
+    rc_t, sig_t, st_t = oracle.OracleBatch(w.networks, w.strategies, timing=True).run(
+        w.F, n_threads=3)
+    assert rc == rc_t == 0
+    np.testing.assert_array_equal(st["steps"], st_t["steps"])
+    assert np.abs(sig_t - sig).max() <= 1e-9 * np.abs(sig).max()

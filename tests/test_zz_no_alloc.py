@@ -17,6 +17,8 @@ alone in a fresh process or after the other tests.
 import numpy as np
 import pytest
 
+from conftest import network_2_7
+
 pytestmark = pytest.mark.gpu
 
 
@@ -60,7 +62,7 @@ def test_noalloc_solve_matches_allocating_solve_twice_in_a_row(lib_path):
     np.testing.assert_array_equal(alloc.current_stress(), noalloc.current_stress())
 
 
-def test_noalloc_relax_mode_and_non_updating_run(lib_path):
+def test_noalloc_relax_mode_and_non_updating_run(lib_path, golden_2_7):
     """RELAX mode (the reference's algorithm): RVEs that converge and one
     stopped by its step cap (status MFG_E_NOT_CONVERGED), an updating run,
     then a non-updating run with one broadcast F and no status output. The
@@ -72,16 +74,22 @@ def test_noalloc_relax_mode_and_non_updating_run(lib_path):
     from mumfim_gb300 import synthetic as S
 
     R = 3
-    w = S.config1(n_rve=R, n_nodes=600)
-    strat = [m.SolutionStrategy(visc_damp_coeff=2.0, residual_tol=1e-9, max_steps=3000),
-             m.SolutionStrategy(visc_damp_coeff=2.0, residual_tol=1e-9, max_steps=3000),
-             m.SolutionStrategy(visc_damp_coeff=0.5, residual_tol=1e-30, max_steps=250)]
-    alloc = m.BatchedFiberRVEAnalysisExplicit(w.networks, strat)
-    noalloc = m.BatchedFiberRVEAnalysisExplicit(w.networks, strat)
+    # Network_2_7 with its damping converges (in about 20,600 steps); the
+    # third RVE is stopped by its step cap
+    net = network_2_7(golden_2_7)
+    w = S.config1(n_rve=1, n_nodes=600)
+    nets = [net, net, w.networks[0]]
+    strat = [m.SolutionStrategy(visc_damp_coeff=golden_2_7["visc_damp_coeff"], residual_tol=1e-6,
+                                max_steps=40_000)] * 2 + [
+        m.SolutionStrategy(visc_damp_coeff=0.5, residual_tol=1e-30, max_steps=250)]
+    alloc = m.BatchedFiberRVEAnalysisExplicit(nets, strat)
+    noalloc = m.BatchedFiberRVEAnalysisExplicit(nets, strat)
+    F_gold = np.array(golden_2_7["F"]).reshape(3, 3)
+    F_all = np.stack([F_gold, F_gold.T, w.F[0]])
     dev = torch.device("cuda", 0)
     stream = torch.cuda.Stream(dev)
     with torch.cuda.stream(stream):
-        F1 = torch.from_numpy(np.ascontiguousarray(w.F.reshape(R, 9))).to(dev)
+        F1 = torch.from_numpy(np.ascontiguousarray(F_all.reshape(R, 9))).to(dev)
         tilt = np.eye(3) + 0.01 * np.array([[0.0, 1.0, 0.0], [0.0, 0.0, 0.0], [0.0, 0.0, -1.0]])
         F2 = torch.from_numpy(np.ascontiguousarray(tilt.reshape(1, 9))).to(dev)
         st_a = torch.zeros((R, 2), dtype=torch.float64, device=dev)
@@ -111,6 +119,7 @@ def test_noalloc_relax_mode_and_non_updating_run(lib_path):
     assert bool(torch.isfinite(s_n2).all())
     for r in range(R):
         np.testing.assert_array_equal(noalloc.displacements(r), u_before[r])
+        np.testing.assert_array_equal(alloc.displacements(r), u_before[r])
         np.testing.assert_array_equal(alloc.displacements(r), noalloc.displacements(r))
         np.testing.assert_array_equal(alloc.coordinates(r), noalloc.coordinates(r))
     np.testing.assert_array_equal(noalloc.current_stress(), cur_before)
