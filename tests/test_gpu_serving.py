@@ -161,3 +161,35 @@ def test_cluster_lane_holds_requests_per_rve(lib_path):
         np.testing.assert_array_equal(by_ticket[a]["sigma"], s1[rve])
         np.testing.assert_array_equal(by_ticket[b]["sigma"], s2[rve])
         assert by_ticket[b]["t_claim_ns"] >= by_ticket[a]["t_done_ns"]
+
+
+@pytest.mark.parametrize("precision", ["f64", "mixed"])
+def test_served_stiffness_equals_batch_run_then_stiffness(lib_path, precision):
+    """A request with stiffness=True returns a full micro_fo_result: the
+    stress of its (updating) solve and the material stiffness of the six
+    perturbed solves that follow it on the same CTA or cluster, bit-identical
+    to mfg_batch_run followed by a sequential mfg_batch_material_stiffness.
+    RVEs of 1,000 - 9,000 nodes: the mixed server solves the largest with
+    4-CTA clusters. A request without the flag reports stiffness_status -1."""
+    import mumfim_gb300 as m
+    from mumfim_gb300 import synthetic as S
+    from mumfim_gb300.serving import RVEServer
+    w = S.config2(n_rve=6, steps=500, n_min=1_000, n_max=9_000)
+    g = m.BatchedFiberRVEAnalysisExplicit(w.networks, w.strategies, precision=precision,
+                                          stiffness="sequential")
+    s_ref = np.zeros((w.n_rve, 6))
+    g.run(w.F, s_ref, update_coords=True)
+    C_ref = g.computeMaterialStiffness()
+    with RVEServer(w.networks, w.strategies, precision=precision) as sv:
+        for r in range(w.n_rve):
+            sv.submit(r, w.F[r], update_coords=True, stiffness=True)
+        res = sv.drain()
+        sv.submit(0, np.eye(3), update_coords=False)
+        plain = sv.drain()
+    assert len(res) == w.n_rve
+    for rec in res:
+        r = int(rec["rve"])
+        assert rec["status"] == 0 and rec["stiffness_status"] == 0
+        np.testing.assert_array_equal(rec["sigma"], s_ref[r])
+        np.testing.assert_array_equal(rec["C"], C_ref[r])
+    assert plain["stiffness_status"][0] == -1 and not plain["C"][0].any()

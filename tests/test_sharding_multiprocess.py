@@ -73,9 +73,12 @@ def _liveness_worker(rank, world, port, q):
         q.put((rank, None, time.monotonic() - t0))
     except sharding.RankFailure as e:
         q.put((rank, e.missing, time.monotonic() - t0))
-    # the survivors meet once more, so rank 0 keeps the store's server up
-    # until rank 1 is done with it
-    sharding.await_peers(store, "done", rank, 2, timeout_s=30)
+    # rank 0 hosts the store's server: it stays up until rank 1's last store
+    # operation has been acknowledged
+    if rank == 1:
+        store.set("bye/1", b"1")
+    else:
+        store.wait(["bye/1"], timedelta(seconds=30))
 
 
 def test_dead_rank_is_detected_between_steps():
