@@ -177,12 +177,24 @@ __global__ void mixed_prepare_fibers_kernel(const DevBatch b, MixedState ms) {
   }
 }
 
-// Fiber data of the node-centric incidences (fiber -1: padding).
+// Fiber data of the node-centric incidences (fiber -1: padding), oriented
+// from the other end to the incidence's node: X[n2] - X[n1] at the fiber's
+// second end, its negation at the first. The set-up codes carry the end in
+// bit 0; the solve needs only the other end's node code, so it is shifted
+// out here.
 __global__ void mixed_prepare_sell_kernel(const MixedState ms, const int64_t* nfib, int64_t n) {
   const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   if (i < n) {
     const int64_t e = nfib[i];
-    ms.nfc[i] = e >= 0 ? ms.fcon[e] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int code = ms.ncode[i];
+    float4 fc = e >= 0 ? ms.fcon[e] : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (!(code & 1)) {
+      fc.x = -fc.x;
+      fc.y = -fc.y;
+      fc.z = -fc.z;
+    }
+    ms.nfc[i] = fc;
+    ms.ncode[i] = code >> 1;
   }
 }
 
@@ -423,11 +435,14 @@ __device__ __forceinline__ NodeConst load_node(const Rve& r, int i) {
   return {__ldg(r.rowptr + i), __ldg(r.rowptr + i + 1), __ldg(r.mass + i)};
 }
 
-// Force vector of one fiber. The displacement difference du is formed with a
-// TwoSum of the hi parts plus the lo parts, so it is accurate to FP32 of du
-// itself; the Green strain follows from du (g l0^2 = du.(dX + du/2)), which
-// keeps its relative precision at small strain where 0.5(l^2/l0^2 - 1)
-// would cancel.
+// Force vector of one fiber. The displacement difference du is the
+// difference of the hi parts plus the difference of the lo parts. Where the
+// two hi parts are within a factor of two of each other -- every short
+// fiber, whose end displacements nearly agree -- their FP32 difference is
+// exact (Sterbenz); elsewhere its rounding is within one ulp of du itself.
+// So du is accurate to FP32 of du, not of u, and the Green strain formed
+// from it (g l0^2 = du.(dX + du/2)) keeps its relative precision at small
+// strain, where 0.5(l^2/l0^2 - 1) would cancel.
 // Returns the current length l0 sqrt(1 + 2g), which the critical time step
 // needs every 100 steps (unused, and so not computed, on the other steps).
 //
@@ -435,11 +450,8 @@ __device__ __forceinline__ NodeConst load_node(const Rve& r, int i) {
 // vector from either end) runs exactly the same arithmetic.
 __device__ __forceinline__ void disp_diff(const NodeRec& na, const NodeRec& nb, float du[3]) {
 #pragma unroll
-  for (int q = 0; q < 3; ++q) {
-    float d, ed;
-    two_sum(nb.hi[q], -na.hi[q], d, ed);
-    du[q] = d + (ed + (nb.lo[q] - na.lo[q]));
-  }
+  for (int q = 0; q < 3; ++q)
+    du[q] = __fadd_rn(__fsub_rn(nb.hi[q], na.hi[q]), __fsub_rn(nb.lo[q], na.lo[q]));
 }
 __device__ __forceinline__ float green(const float du[3], const float4& fc) {
   const float gn = fmaf(du[0], fmaf(0.5f, du[0], fc.x),
@@ -822,8 +834,17 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
 // slices of 32, a slice as wide as its largest degree, and the k-th
 // incidence of the node at lane l of a slice is at slice base + 32 k + l. A
 // warp's loads of incidence codes and fiber data are then contiguous. An
-// incidence holds (other end's node code << 1 | 1 if this node is the
-// fiber's second end) and the fiber's (X[n2] - X[n1], 1 / l0).
+// incidence holds the other end's node code and the fiber's (X_me - X_o,
+// 1 / l0): its reference difference oriented from the other end to this
+// node (mixed_prepare_sell_kernel).
+//
+// With both differences taken from the other end to this node, the vector
+// (dX + du) T / l is the fiber's force vector at its second end and exactly
+// its negation at the first: the TwoSum difference of the negated operands
+// is the negated difference (rounding to nearest is symmetric), the Green
+// strain is unchanged under (dX, du) -> (-dX, -du), and so is T / l. Adding
+// it is the same rounding as subtracting the second-end vector, so the sums
+// are the bits the fiber-centric solve gathers.
 
 // Internal force of one node with record `me` from its deg incidences
 // starting at p.
@@ -844,17 +865,16 @@ __device__ __forceinline__ void nodal_force(const Law& L, const Nodes& u, const 
       cn = __ldg(ncode + p);
       fcn = __ldg(nfc + p);
     }
-    const NodeRec o = u.load(c >> 1);
-    const float sg = (c & 1) ? 1.f : -1.f;
+    const NodeRec o = u.load(c);
     float du[3];
-    disp_diff(o, me, du);  // x_me - x_o: the fiber's du at its second end
-#pragma unroll
-    for (int q = 0; q < 3; ++q) du[q] *= sg;
+    disp_diff(o, me, du);  // x_me - x_o
     const float g = green(du, fc);
     const float4 f = force_vec(L, du, fc, g);
-    a0 = fmaf(sg, f.x, a0);
-    a1 = fmaf(sg, f.y, a1);
-    a2 = fmaf(sg, f.z, a2);
+    // an add that is never fused with the product forming f: the vector is
+    // rounded before it is summed, as when the fiber-centric solve gathers it
+    a0 = __fadd_rn(a0, f.x);
+    a1 = __fadd_rn(a1, f.y);
+    a2 = __fadd_rn(a2, f.z);
     if (!more) break;
     c = cn;
     fc = fcn;
