@@ -455,6 +455,8 @@ def main():
     ap.add_argument("--serve-steps", type=int, default=500)
     ap.add_argument("--config3-every", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--small-rves-per-cta", type=int, default=0,
+                    help="mixed: small RVEs solved side by side per CTA (1 or 2; 0 = 2)")
     ap.add_argument("--autotune", action="store_true",
                     help="mixed: time 100-step solves under each cluster-size limit first and "
                          "use the fastest (mumfim_gb300.autotune)")
@@ -496,7 +498,8 @@ def main():
     t0 = time.perf_counter()
     gpu = m.BatchedFiberRVEAnalysisExplicit(w.networks, w.strategies, precision=args.precision,
                                             device=local_rank,
-                                            max_cluster_ctas=tune["max_cluster_ctas"] if tune else 0)
+                                            max_cluster_ctas=tune["max_cluster_ctas"] if tune else 0,
+                                            small_rves_per_cta=args.small_rves_per_cta)
     setup_s = time.perf_counter() - t0
     R = w.n_rve
     fiber_steps = w.total_fibers * w.steps

@@ -125,7 +125,10 @@ typedef struct mfg_options {
                                clusters; the results are the same either way. */
   int32_t stiffness;        /* mfg_stiffness_solves: how mfg_batch_material_stiffness()
                                runs its six perturbed solves */
-  int32_t reserved[2];
+  int32_t small_rves_per_cta; /* mixed precision: how many small RVEs (whole state within
+                               half a CTA's shared memory) one CTA solves side by side,
+                               1 or 2 (0 = 2); the results are the same either way */
+  int32_t reserved[1];
 } mfg_options;
 
 /* The six perturbed solves of mfg_batch_material_stiffness(). The reference

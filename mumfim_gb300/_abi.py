@@ -52,7 +52,7 @@ class mfg_options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("device", C.c_int32),
                 ("threads_per_rve", C.c_int32), ("max_cluster_ctas", C.c_int32),
                 ("cluster_layout", C.c_int32), ("stiffness", C.c_int32),
-                ("reserved", C.c_int32 * 2)]
+                ("small_rves_per_cta", C.c_int32), ("reserved", C.c_int32 * 1)]
 
 
 class mfg_rve_status(C.Structure):

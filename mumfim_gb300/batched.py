@@ -118,11 +118,12 @@ class BatchedFiberRVEAnalysisExplicit:
     stiffness   "auto", "sequential" or "concurrent": how computeMaterialStiffness
                 runs its six perturbed solves (mfg_stiffness_solves in
                 include/mumfim_gpu.h)
+    small_rves_per_cta  mixed precision: 1 or 2 small RVEs per CTA (0 = 2); same results
     """
 
     def __init__(self, networks: Sequence, strategies: Sequence, precision: str = "f64",
                  device: int = 0, max_cluster_ctas: int = 0, serving_layout: bool = False,
-                 stiffness: str = "auto"):
+                 stiffness: str = "auto", small_rves_per_cta: int = 0):
         L = load_library()
         if len(networks) != len(strategies):
             raise ValueError("There must be a solution strategy for each fiber network!")
@@ -133,6 +134,7 @@ class BatchedFiberRVEAnalysisExplicit:
         opts.max_cluster_ctas = max_cluster_ctas
         opts.cluster_layout = 1 if serving_layout else 0
         opts.stiffness = _abi.MFG_STIFFNESS[stiffness]
+        opts.small_rves_per_cta = small_rves_per_cta
         h = C.c_void_p()
         _check(L.mfg_batch_create(self._arr.nets, self._arr.strats, len(networks), C.byref(opts),
                                   C.byref(h)))

@@ -486,6 +486,9 @@ mfg_status mfg_batch_create(const mfg_network* nets, const mfg_strategy* strateg
   if (opt.cluster_layout != MFG_LAYOUT_BATCH && opt.cluster_layout != MFG_LAYOUT_SERVING)
     return fail(MFG_E_INVALID, "cluster_layout must be MFG_LAYOUT_BATCH or MFG_LAYOUT_SERVING "
                 "(got %d)", opt.cluster_layout);
+  if (opt.small_rves_per_cta < 0 || opt.small_rves_per_cta > 2)
+    return fail(MFG_E_INVALID, "small_rves_per_cta must be 0, 1 or 2 (got %d)",
+                opt.small_rves_per_cta);
   if (opt.stiffness != MFG_STIFFNESS_AUTO && opt.stiffness != MFG_STIFFNESS_SEQUENTIAL &&
       opt.stiffness != MFG_STIFFNESS_CONCURRENT)
     return fail(MFG_E_INVALID, "stiffness must be MFG_STIFFNESS_AUTO, _SEQUENTIAL or _CONCURRENT "
@@ -669,7 +672,8 @@ mfg_status mfg_batch_create(const mfg_network* nets, const mfg_strategy* strateg
     cudaError_t e =
         b->mixed ? mfg::mixed_create(*b->mixed, dv, b->desc, conn, rowptr, inc, b->sms,
                                      opt.max_cluster_ctas > 0 ? opt.max_cluster_ctas : 8,
-                                     opt.cluster_layout == MFG_LAYOUT_SERVING, s)
+                                     opt.cluster_layout == MFG_LAYOUT_SERVING,
+                                     opt.small_rves_per_cta > 0 ? opt.small_rves_per_cta : 2, s)
                  : cudaErrorMemoryAllocation;
     if (e != cudaSuccess)
       return fail(e == cudaErrorMemoryAllocation ? MFG_E_OOM : MFG_E_CUDA,

@@ -61,7 +61,7 @@ namespace mfg {
 // arguments, and the run-time placement's global scratch. Context 0 serves
 // the batch's runs; contexts 1-6 the concurrent perturbed solves of the
 // material stiffness, which run at the same time on the same batch.
-constexpr int kMixedBuckets = 6;
+constexpr int kMixedBuckets = 7;
 struct MixedRunCtx {
   int32_t* queues = nullptr;  // one claim counter per bucket (device)
   float* u_hl = nullptr;      // run-time placement scratch; null: the batch's own
@@ -117,8 +117,8 @@ struct MixedState {
   // RVEs of bucket q, most fibers first, are order[bucket_off[q] ..
   // bucket_off[q + 1]).
   int32_t* order = nullptr;
-  int bucket_off[7] = {};
-  int bucket_grid[6] = {};
+  int bucket_off[kMixedBuckets + 1] = {};
+  int bucket_grid[kMixedBuckets] = {};
   // Run contexts (host memory; kernels never touch this pointer). A run is a
   // CUDA graph (queue reset, fork, one launch per bucket, join), captured
   // per context for the last run arguments and replayed while they stay
@@ -135,17 +135,21 @@ struct BucketKind {
   int cl;      // CTAs per cluster
   bool all;    // fiber-centric: force vectors in shared memory too
   bool nodal;  // node-centric solve (node state in shared memory)
+  int ng;      // RVEs solved side by side by one CTA (fiber-centric, all on chip)
 };
 constexpr int kBuckets = kMixedBuckets;
-constexpr BucketKind kBucket[kBuckets] = {{8, false, true}, {4, false, true}, {2, false, true},
-                                          {1, false, true}, {1, true, false}, {1, false, false}};
+constexpr BucketKind kBucket[kBuckets] = {{8, false, true, 1}, {4, false, true, 1},
+                                          {2, false, true, 1}, {1, false, true, 1},
+                                          {1, true, false, 1}, {1, true, false, 2},
+                                          {1, false, false, 1}};
 // Placement preference (bucket_of): the first bucket whose shared memory
 // holds the RVE, else the last bucket.
-constexpr int kPref[] = {4, 3, 2, 1, 0};
+constexpr int kPref[] = {5, 4, 3, 2, 1, 0};
 // The single-CTA buckets with an RVE order of their own, by kind.
-constexpr int kQNodal1 = 3, kQFiberAll = 4;
+constexpr int kQNodal1 = 3, kQFiberAll = 4, kQFiberPair = 5;
 static_assert(kBucket[kQNodal1].cl == 1 && kBucket[kQNodal1].nodal, "bucket table");
 static_assert(kBucket[kQFiberAll].cl == 1 && kBucket[kQFiberAll].all, "bucket table");
+static_assert(kBucket[kQFiberPair].all && kBucket[kQFiberPair].ng == 2, "bucket table");
 
 __global__ void mixed_prepare_kernel(const DevBatch b, MixedState ms) {
   const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
@@ -379,6 +383,87 @@ struct ClusterOps {
   }
 };
 
+// The threads that solve one RVE: the whole CTA (NG = 1) or one of NG equal
+// groups of it, each synchronised by its own named barrier (barrier 0 is
+// the CTA's), so that small RVEs can share a CTA without waiting for each
+// other.
+template <int NG>
+struct Group {
+  static_assert(NG == 1 || NG == 2, "one or two RVEs per CTA");
+  static constexpr int kSize = kThreadsMixed / NG;
+  __device__ static int index() { return NG == 1 ? 0 : static_cast<int>(threadIdx.x) / kSize; }
+  __device__ static int tid() {
+    return NG == 1 ? static_cast<int>(threadIdx.x) : static_cast<int>(threadIdx.x) % kSize;
+  }
+  __device__ static void sync() {
+    if constexpr (NG == 1)
+      __syncthreads();
+    else
+      asm volatile("bar.sync %0, %1;" ::"r"(1 + index()), "r"(kSize) : "memory");
+  }
+};
+
+// Minimum over a group (min is exact, so the order does not matter).
+template <int NG>
+__device__ __forceinline__ double group_min(double v, double* red) {
+  if constexpr (NG == 1) {
+    return block_min<kThreadsMixed>(v, red);
+  } else {
+    constexpr int NW = Group<NG>::kSize / 32;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int w = Group<NG>::tid() >> 5, l = threadIdx.x & 31;
+    Group<NG>::sync();
+    if (l == 0) red[w] = v;
+    Group<NG>::sync();
+    if (w == 0) {
+      double t = (l < NW) ? red[l] : DBL_MAX;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t = fmin(t, __shfl_xor_sync(0xffffffffu, t, o));
+      if (l == 0) red[NW] = t;
+    }
+    Group<NG>::sync();
+    return red[NW];
+  }
+}
+
+// Sum over kThreadsMixed "virtual threads" in the fixed order of
+// block_sum<kThreadsMixed>: thread t of a group of kSize threads holds the
+// partial sums acc[j] of virtual threads t + j kSize. Each virtual warp is
+// reduced by the same butterfly over the same lanes, and its partial lands
+// in the same slot, so a group of any size gives the bits of a whole CTA.
+template <int NG>
+__device__ __forceinline__ double group_sum(const double (&acc)[NG], double* red) {
+  if constexpr (NG == 1) {
+    return block_sum<kThreadsMixed>(acc[0], red);
+  } else {
+    constexpr int NWV = kThreadsMixed / 32;       // virtual warps
+    constexpr int NWG = Group<NG>::kSize / 32;    // warps of the group
+    double v[NG];
+#pragma unroll
+    for (int j = 0; j < NG; ++j) {
+      v[j] = acc[j];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_xor_sync(0xffffffffu, v[j], o);
+    }
+    const int w = Group<NG>::tid() >> 5, l = threadIdx.x & 31;
+    Group<NG>::sync();
+    if (l == 0) {
+#pragma unroll
+      for (int j = 0; j < NG; ++j) red[w + j * NWG] = v[j];
+    }
+    Group<NG>::sync();
+    if (w == 0) {
+      double t = (l < NWV) ? red[l] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      if (l == 0) red[NWV] = t;
+    }
+    Group<NG>::sync();
+    return red[NWV];
+  }
+}
+
 // Nodal internal force: incident fiber vectors in the node's CSR order,
 // subtracted at a fiber's first end and added at its second.
 template <class Forces>
@@ -477,17 +562,17 @@ __device__ __forceinline__ float fiber_force(const Rve& r, const Nodes& u, int e
   return fiber_length(g, k.fc.w);
 }
 
-// Force vectors of fiber slots e_lo + tid, + kThreadsMixed, ... < e_hi, the
+// Force vectors of fiber slots e_lo + tid, + group size, ... < e_hi, the
 // next slot's read-only data loaded while the current one is computed.
 // Returns the shortest current length among them when kLen.
-template <bool kLen, class Nodes>
+template <bool kLen, int NG = 1, class Nodes>
 __device__ __forceinline__ float fiber_pass(const Rve& r, const Nodes& u, int e_lo, int e_hi) {
   float lmin = FLT_MAX;
-  int e = e_lo + static_cast<int>(threadIdx.x);
+  int e = e_lo + Group<NG>::tid();
   if (e >= e_hi) return lmin;
   FiberConst cur = load_fiber(r, e);
   for (;;) {
-    const int en = e + kThreadsMixed;
+    const int en = e + Group<NG>::kSize;
     const bool more = en < e_hi;
     FiberConst nxt = cur;
     if (more) nxt = load_fiber(r, en);
@@ -505,13 +590,15 @@ __device__ __forceinline__ float fiber_pass(const Rve& r, const Nodes& u, int e_
 // boundary nodes: each thread sums a strided share in the reference's
 // boundary order, then a fixed-order block reduction. The FP64 kernel keeps
 // the reference's serial sum; here any fixed order will do, and it keeps the
-// result independent of what else runs. One component at a time keeps one
-// accumulator live.
+// result independent of what else runs (and of the group size: group_sum
+// keeps the order of a whole CTA). One component at a time keeps NG
+// accumulators live.
+template <int NG = 1>
 __device__ __forceinline__ void mixed_stress(const DevBatch& b, const RunArgs& a, int rve,
                                              int status, int step, double residual, double* red,
                                              bool leader) {
   const RveDesc& d = b.desc[rve];
-  const int tid = threadIdx.x;
+  const int tid = Group<NG>::tid();
   const int64_t no = d.node_off, nt = b.nt;
   const int32_t* bo = b.bnd + d.bnd_off;
   const int nb = leader ? d.n_nodes - d.n_free : 0;  // every CTA reduces, one sums
@@ -526,12 +613,18 @@ __device__ __forceinline__ void mixed_stress(const DevBatch& b, const RunArgs& a
     const double* xj = b.x + cj * nt + no;
     const double* fi = b.fint + ci * nt + no;
     const double* fj = b.fint + cj * nt + no;
-    double acc = 0.0;
-    for (int q = tid; q < nb; q += kThreadsMixed) {
+    // virtual thread t + j kSize sums q = t + j kSize + m kThreadsMixed
+    double acc[NG];
+#pragma unroll
+    for (int j = 0; j < NG; ++j) acc[j] = 0.0;
+    for (int q = tid, j = 0; q < nb; q += Group<NG>::kSize, j = (j + 1 == NG ? 0 : j + 1)) {
       const int i = bo[q];
-      acc += k < 3 ? xi[i] * fi[i] : 0.5 * (xi[i] * fj[i] + xj[i] * fi[i]);
+      const double t = k < 3 ? xi[i] * fi[i] : 0.5 * (xi[i] * fj[i] + xj[i] * fi[i]);
+#pragma unroll
+      for (int jj = 0; jj < NG; ++jj)
+        if (jj == j) acc[jj] += t;
     }
-    const double sk = block_sum<kThreadsMixed>(acc, red) * sc;
+    const double sk = group_sum<NG>(acc, red) * sc;
     bad = bad || !isfinite(sk);
     if (leader && tid == 0) {
       a.sigma[6 * rve + k] = sk;
@@ -561,15 +654,15 @@ __host__ __device__ inline int64_t cluster_floats(int n_nodes, int n_free, int n
 // (BatchedFiberRVEAnalysisExplicitBase.h:16-57) or, in RAMP mode, the
 // boundary's per-step increment; displacements split into (hi, lo); v = 0.
 // kOrder: the RVE has its own node order (gnode maps positions to nodes).
-template <bool kOrder>
+template <bool kOrder, int NG = 1>
 __device__ __forceinline__ void mixed_prologue(const DevBatch& b, const MixedState& ms,
                                                const Rve& r, const double Fm[9], bool ramp,
                                                int f_lo, int g_lo, int nfo, int n_own, int fchunk,
                                                const LocalNodes& own, float* vel) {
   const RveDesc& d = r.d;
-  const int NF = d.n_free, tid = threadIdx.x;
+  const int NF = d.n_free, tid = Group<NG>::tid();
   const int64_t no = d.node_off, nt = b.nt;
-  for (int t = tid; t < n_own; t += kThreadsMixed) {
+  for (int t = tid; t < n_own; t += Group<NG>::kSize) {
     const int i = t < nfo ? f_lo + t : g_lo + (t - nfo);
     const int li = t < nfo ? t : fchunk + (t - nfo);
     const int64_t gi = kOrder ? __ldg(ms.gnode + no + i) : no + i;  // batch node index
@@ -616,10 +709,11 @@ __device__ __forceinline__ void mixed_prologue(const DevBatch& b, const MixedSta
 }
 
 // RAMP mode: the own boundary nodes move by their exact (hi, lo) increment.
+template <int NG = 1>
 __device__ __forceinline__ void ramp_boundary(const Rve& r, const LocalNodes& own, int g_lo,
                                               int g_hi, int fchunk) {
   const int NF = r.d.n_free;
-  for (int i = g_lo + static_cast<int>(threadIdx.x); i < g_hi; i += kThreadsMixed) {
+  for (int i = g_lo + Group<NG>::tid(); i < g_hi; i += Group<NG>::kSize) {
     const float* rb = r.ramp + 12 * (i - NF);
     float* rec = own.rec(fchunk + (i - g_lo));
     NodeRec nr = load_rec(rec);
@@ -641,20 +735,21 @@ __device__ __forceinline__ void ramp_boundary(const Rve& r, const LocalNodes& ow
 // order (cluster_order); without kAll it places the RVE by its size at run
 // time, in the batch's order: everything in shared memory, the node state
 // only, the displacements only, or everything in global memory.
-template <bool kAll>
+template <bool kAll, int NG = 1>
 __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const RunArgs& a, int rve,
-                                double* red, double* cred, float* smem, int smem_floats) {
-  using Ops = ClusterOps<1>;
+                                double* red, float* smem, int smem_floats) {
+  static_assert(NG == 1 || kAll, "RVEs share a CTA only when their state fits its shared memory");
+  using G = Group<NG>;  // the threads solving this RVE
   Rve r;
   r.d = b.desc[rve];
   const RveDesc& d = r.d;
   r.L = make_law(d);
   const int N = d.n_nodes, NF = d.n_free, E = d.n_fibers;
-  const int tid = threadIdx.x;
+  const int tid = G::tid();
   const int64_t no = d.node_off, fo = d.fiber_off, nt = b.nt;
   r.node_off = no;
   r.nt = nt;
-  // the CTA owns every node (free [0, NF), boundary [NF, N), local index =
+  // the group owns every node (free [0, NF), boundary [NF, N), local index =
   // node position) and every fiber slot
   const int rank = 0;
   const int f_lo = 0, f_hi = NF, g_lo = NF, g_hi = N, nfo = NF, n_own = N, fchunk = NF;
@@ -705,13 +800,12 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   if (a.update_coords && rank == 0 && tid == 0) b.vol[rve] = jacobian(Fm) * b.vol[rve];
 
   // ---- prologue in FP64: predictor, split into (hi, lo), v = 0 -------------
-  mixed_prologue<kAll>(b, ms, r, Fm, ramp, f_lo, g_lo, nfo, n_own, fchunk, own, vel);
-  Ops::sync();
+  mixed_prologue<kAll, NG>(b, ms, r, Fm, ramp, f_lo, g_lo, nfo, n_own, fchunk, own, vel);
+  G::sync();
   // critical step from the shortest current fiber (FP32 length from the
   // Green strain, ~1e-7 relative; h itself is an FP32 number)
-  const float lmin = fiber_pass<true>(r, u, e_lo, e_hi);
-  double dt_crit =
-      Ops::template combine<true>(block_min<kThreadsMixed>(lmin, red), cred) / d.sound_speed;
+  const float lmin = fiber_pass<true, NG>(r, u, e_lo, e_hi);
+  double dt_crit = group_min<NG>(lmin, red) / d.sound_speed;
 
   const int step_cap = d.max_steps;
   const float c = static_cast<float>(d.c);
@@ -723,14 +817,20 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   for (;;) {
     const bool res_step = step > 0 && ((step - 1) % kUpdateFreq) == 0;
     if (res_step) {
-      double part = 0.0;
-      for (int i = f_lo + tid; i < f_hi; i += kThreadsMixed) {
+      // virtual thread tid + j kSize sums the nodes tid + j kSize + m kThreadsMixed
+      double part[NG];
+#pragma unroll
+      for (int j = 0; j < NG; ++j) part[j] = 0.0;
+      for (int i = f_lo + tid, j = 0; i < f_hi; i += G::kSize, j = (j + 1 == NG ? 0 : j + 1)) {
         float a0, a1, a2;
         gather(r, fv, i, a0, a1, a2);
-        part += static_cast<double>(a0) * a0 + static_cast<double>(a1) * a1 +
-                static_cast<double>(a2) * a2;
+        const double q2 = static_cast<double>(a0) * a0 + static_cast<double>(a1) * a1 +
+                          static_cast<double>(a2) * a2;
+#pragma unroll
+        for (int jj = 0; jj < NG; ++jj)
+          if (jj == j) part[jj] += q2;
       }
-      residual = sqrt(Ops::template combine<false>(block_sum<kThreadsMixed>(part, red), cred));
+      residual = sqrt(group_sum<NG>(part, red));
       if (!isfinite(residual)) {
         status = 4;
         break;
@@ -748,7 +848,7 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
       int i = f_lo + tid;
       NodeConst cur = load_node(r, i);
       for (;;) {
-        const int in = i + kThreadsMixed;
+        const int in = i + G::kSize;
         const bool more = in < f_hi;
         NodeConst nxt = cur;
         if (more) nxt = load_node(r, in);
@@ -772,17 +872,16 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
         i = in;
       }
     }
-    if (ramp) ramp_boundary(r, own, g_lo, g_hi, fchunk);
-    Ops::sync();
+    if (ramp) ramp_boundary<NG>(r, own, g_lo, g_hi, fchunk);
+    G::sync();
     const bool dt_step = (step % kUpdateFreq) == 0;
     if (dt_step) {
-      const float lm = fiber_pass<true>(r, u, e_lo, e_hi);
-      dt_crit =
-          Ops::template combine<true>(block_min<kThreadsMixed>(lm, red), cred) / d.sound_speed;
+      const float lm = fiber_pass<true, NG>(r, u, e_lo, e_hi);
+      dt_crit = group_min<NG>(lm, red) / d.sound_speed;
       h_cur = static_cast<float>(d.crit * dt_crit * 0.5);
     } else {
-      fiber_pass<false>(r, u, e_lo, e_hi);
-      Ops::sync();
+      fiber_pass<false, NG>(r, u, e_lo, e_hi);
+      G::sync();
     }
     h_prev = h;
     ++step;
@@ -790,7 +889,7 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   if (status == 0 && !ramp && residual > d.tol) status = 3;
 
   // ---- finalize: FP64 positions, boundary f_int, stress ---------------------
-  for (int t = tid; t < n_own; t += kThreadsMixed) {
+  for (int t = tid; t < n_own; t += G::kSize) {
     const int i = t < nfo ? f_lo + t : g_lo + (t - nfo);
     const int li = t < nfo ? t : fchunk + (t - nfo);
     const int64_t gi = kAll ? __ldg(ms.gnode + no + i) : no + i;  // batch node index
@@ -810,9 +909,9 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
       b.fint[2 * nt + no + i] = a2;
     }
   }
-  Ops::sync();
-  mixed_stress(b, a, rve, status, step, residual, red, rank == 0);
-  Ops::sync();
+  G::sync();
+  mixed_stress<NG>(b, a, rve, status, step, residual, red, rank == 0);
+  G::sync();
 }
 
 // ---- node-centric solve -----------------------------------------------------
@@ -1085,37 +1184,43 @@ __device__ void solve_rve_nodal(const DevBatch& b, const MixedState& ms, const R
 
 // Persistent relaxation over one size bucket: CTA (or cluster) after cluster
 // takes the next RVE of `order` (largest first) until the bucket is empty.
-template <int CL, bool kAll, bool kNodal>
+// With NG = 2 each half of the CTA is a group that takes RVEs on its own,
+// in half of the shared memory, synchronised by its own named barrier.
+template <int CL, bool kAll, bool kNodal, int NG>
 __global__ void __launch_bounds__(kThreadsMixed, 1)
 relax_mixed_kernel(const DevBatch b, const MixedState ms, const RunArgs a, int smem_floats,
                    const int32_t* order, int n_order, int32_t* queue) {
   static_assert(kNodal || CL == 1, "the fiber-centric solve runs on one CTA");
+  static_assert(NG == 1 || (CL == 1 && kAll && !kNodal), "only small fiber-centric RVEs pair up");
+  constexpr int kRed = kThreadsMixed / 32 + 1;
   extern __shared__ float4 smem4[];
   float* smem = reinterpret_cast<float*>(smem4);
-  __shared__ double red[kThreadsMixed / 32 + 1];
+  __shared__ double red[NG * kRed];
   __shared__ double cred[1];
-  __shared__ int s_rve;
+  __shared__ int s_rve[NG];
+  const int g = Group<NG>::index();
   for (;;) {
-    if (ClusterOps<CL>::rank() == 0 && threadIdx.x == 0) {
+    if (ClusterOps<CL>::rank() == 0 && Group<NG>::tid() == 0) {
       const int w = atomicAdd(queue, 1);
-      s_rve = w < n_order ? order[w] : -1;
+      s_rve[g] = w < n_order ? order[w] : -1;
     }
     int rve;
     if constexpr (CL > 1) {
       cg::cluster_group cl = cg::this_cluster();
       cl.sync();
-      rve = *cl.map_shared_rank(&s_rve, 0);
+      rve = *cl.map_shared_rank(&s_rve[0], 0);
       cl.sync();
     } else {
-      __syncthreads();
-      rve = s_rve;
-      __syncthreads();
+      Group<NG>::sync();
+      rve = s_rve[g];
+      Group<NG>::sync();
     }
     if (rve < 0) break;
     if constexpr (kNodal)
       solve_rve_nodal<CL>(b, ms, a, rve, red, cred, smem);
     else
-      solve_rve_mixed<kAll>(b, ms, a, rve, red, cred, smem, smem_floats);
+      solve_rve_mixed<kAll, NG>(b, ms, a, rve, red + g * kRed, smem + g * (smem_floats / NG),
+                                smem_floats / NG);
   }
 }
 
@@ -1128,10 +1233,10 @@ __device__ __forceinline__ void serve_one_cta(const DevBatch& b, const MixedStat
   const int q = __ldg(ms.rve_bucket + rve);
   if (q == kQNodal1)
     solve_rve_nodal<1>(b, ms, a, rve, red, cred, smem);
-  else if (q == kQFiberAll)
-    solve_rve_mixed<true>(b, ms, a, rve, red, cred, smem, smem_floats);
+  else if (q == kQFiberAll || q == kQFiberPair)
+    solve_rve_mixed<true>(b, ms, a, rve, red, smem, smem_floats);
   else
-    solve_rve_mixed<false>(b, ms, a, rve, red, cred, smem, smem_floats);
+    solve_rve_mixed<false>(b, ms, a, rve, red, smem, smem_floats);
 }
 
 __global__ void __launch_bounds__(kThreadsMixed, 1)
@@ -1385,14 +1490,34 @@ namespace {
 // clusters of 4 (144 SMs). Clusters above max_cluster CTAs are not used,
 // nor clusters of 2 in the serving layout (the serving kernel solves in
 // clusters of 4 only).
-int bucket_of(const RveDesc& d, int smem_floats, int max_cluster, bool serving_layout) {
+// Small RVEs whose whole state fits half a CTA's shared memory come first:
+// two of them share a CTA (at most rves_per_cta).
+int bucket_of(const RveDesc& d, int smem_floats, int max_cluster, bool serving_layout,
+              int rves_per_cta) {
   for (int q : kPref)
     if (kBucket[q].cl <= max_cluster && !(serving_layout && kBucket[q].cl == 2) &&
+        kBucket[q].ng <= rves_per_cta &&
         cluster_floats(d.n_nodes, d.n_free, d.n_fibers, kBucket[q].cl,
-                       kBucket[q].all && !kBucket[q].nodal) <= smem_floats)
+                       kBucket[q].all && !kBucket[q].nodal) <= smem_floats / kBucket[q].ng)
       return q;
   return kBuckets - 1;
 }
+
+// Calls fn(std::integral_constant<int, q>{}) for the run-time bucket index q.
+template <class Fn>
+cudaError_t with_bucket(int q, Fn&& fn) {
+  switch (q) {
+    case 0: return fn(std::integral_constant<int, 0>{});
+    case 1: return fn(std::integral_constant<int, 1>{});
+    case 2: return fn(std::integral_constant<int, 2>{});
+    case 3: return fn(std::integral_constant<int, 3>{});
+    case 4: return fn(std::integral_constant<int, 4>{});
+    case 5: return fn(std::integral_constant<int, 5>{});
+    case 6: return fn(std::integral_constant<int, 6>{});
+    default: return cudaErrorInvalidValue;
+  }
+}
+static_assert(kBuckets == 7, "with_bucket covers every bucket");
 
 template <int CL, bool kAll>
 cudaLaunchConfig_t launch_config(const MixedState& ms, unsigned grid, cudaStream_t s,
@@ -1411,37 +1536,40 @@ cudaLaunchConfig_t launch_config(const MixedState& ms, unsigned grid, cudaStream
   return cfg;
 }
 
-template <int CL, bool kAll, bool kNodal>
-cudaError_t launch_bucket(const MixedState& ms, const DevBatch& b, const RunArgs& a, int q,
+template <int Q>
+cudaError_t launch_bucket(const MixedState& ms, const DevBatch& b, const RunArgs& a,
                           int32_t* queue, cudaStream_t s) {
-  const int n = ms.bucket_off[q + 1] - ms.bucket_off[q];
+  constexpr BucketKind k = kBucket[Q];
+  const int n = ms.bucket_off[Q + 1] - ms.bucket_off[Q];
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg =
-      launch_config<CL, kAll>(ms, static_cast<unsigned>(ms.bucket_grid[q]), s, attr);
-  return cudaLaunchKernelEx(&cfg, relax_mixed_kernel<CL, kAll, kNodal>, b, ms, a,
+      launch_config<k.cl, k.all>(ms, static_cast<unsigned>(ms.bucket_grid[Q]), s, attr);
+  return cudaLaunchKernelEx(&cfg, relax_mixed_kernel<k.cl, k.all, k.nodal, k.ng>, b, ms, a,
                             static_cast<int>(ms.smem_bytes / sizeof(float)),
-                            static_cast<const int32_t*>(ms.order + ms.bucket_off[q]), n, queue);
+                            static_cast<const int32_t*>(ms.order + ms.bucket_off[Q]), n, queue);
 }
 
-template <int CL, bool kAll, bool kNodal>
-cudaError_t setup_bucket(MixedState& ms, int n, int q) {
-  cudaError_t e = cudaFuncSetAttribute(relax_mixed_kernel<CL, kAll, kNodal>,
+template <int Q>
+cudaError_t setup_bucket(MixedState& ms, int n) {
+  constexpr BucketKind k = kBucket[Q];
+  cudaError_t e = cudaFuncSetAttribute(relax_mixed_kernel<k.cl, k.all, k.nodal, k.ng>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        ms.smem_bytes);
   if (e != cudaSuccess) return e;
   int clusters = ms.sms;
-  if (CL > 1 && n > 0) {
+  if (k.cl > 1 && n > 0) {
     cudaLaunchAttribute attr[1];
     cudaLaunchConfig_t cfg =
-        launch_config<CL, kAll>(ms, static_cast<unsigned>(CL * ms.sms), nullptr, attr);
+        launch_config<k.cl, k.all>(ms, static_cast<unsigned>(k.cl * ms.sms), nullptr, attr);
     clusters = 0;
-    if ((e = cudaOccupancyMaxActiveClusters(&clusters, relax_mixed_kernel<CL, kAll, kNodal>,
-                                            &cfg)) !=
-        cudaSuccess)
+    if ((e = cudaOccupancyMaxActiveClusters(&clusters,
+                                            relax_mixed_kernel<k.cl, k.all, k.nodal, k.ng>,
+                                            &cfg)) != cudaSuccess)
       return e;
     if (clusters < 1) return cudaErrorInvalidConfiguration;
   }
-  ms.bucket_grid[q] = CL * std::min(n, clusters);
+  // CTAs (or clusters) for n RVEs at k.ng RVEs each, at most one per SM
+  ms.bucket_grid[Q] = k.cl * std::min((n + k.ng - 1) / k.ng, clusters);
   return cudaSuccess;
 }
 
@@ -1450,7 +1578,7 @@ cudaError_t setup_bucket(MixedState& ms, int n, int q) {
 cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<RveDesc>& desc,
                          const std::vector<int2>& conn, const std::vector<int32_t>& rowptr,
                          const std::vector<int32_t>& inc, int sms, int max_cluster,
-                         bool serving_layout, cudaStream_t s) {
+                         bool serving_layout, int rves_per_cta, cudaStream_t s) {
   cudaError_t e;
   const size_t nt = static_cast<size_t>(b.nt), et = static_cast<size_t>(b.et);
   if ((e = alloc(&ms.u_hl, 6 * nt)) != cudaSuccess) return e;
@@ -1493,7 +1621,7 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
   std::vector<int> rve_q(desc.size());
   ms.h_cl = new int32_t[std::max<size_t>(desc.size(), 1)];
   for (size_t r = 0; r < desc.size(); ++r) {
-    rve_q[r] = bucket_of(desc[r], smem_floats, max_cluster, serving_layout);
+    rve_q[r] = bucket_of(desc[r], smem_floats, max_cluster, serving_layout, rves_per_cta);
     bucket[rve_q[r]].push_back(static_cast<int32_t>(r));
     ms.h_cl[r] = kBucket[rve_q[r]].cl;
   }
@@ -1592,26 +1720,7 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
     return e;
   for (int q = 0; q < kBuckets; ++q) {
     const int n = ms.bucket_off[q + 1] - ms.bucket_off[q];
-    switch (q) {
-      case 0:
-        e = setup_bucket<kBucket[0].cl, kBucket[0].all, kBucket[0].nodal>(ms, n, q);
-        break;
-      case 1:
-        e = setup_bucket<kBucket[1].cl, kBucket[1].all, kBucket[1].nodal>(ms, n, q);
-        break;
-      case 2:
-        e = setup_bucket<kBucket[2].cl, kBucket[2].all, kBucket[2].nodal>(ms, n, q);
-        break;
-      case 3:
-        e = setup_bucket<kBucket[3].cl, kBucket[3].all, kBucket[3].nodal>(ms, n, q);
-        break;
-      case 4:
-        e = setup_bucket<kBucket[4].cl, kBucket[4].all, kBucket[4].nodal>(ms, n, q);
-        break;
-      default:
-        e = setup_bucket<kBucket[5].cl, kBucket[5].all, kBucket[5].nodal>(ms, n, q);
-        break;
-    }
+    e = with_bucket(q, [&](auto Q) { return setup_bucket<decltype(Q)::value>(ms, n); });
     if (e != cudaSuccess) return e;
   }
 
@@ -1675,26 +1784,9 @@ cudaError_t enqueue_buckets(const MixedState& ms, MixedRunCtx& c, const DevBatch
     cudaStream_t sq = c.side[q];
     if ((e = cudaStreamWaitEvent(sq, c.fork, 0)) != cudaSuccess) return e;
     int32_t* queue = c.queues + q;
-    switch (q) {
-      case 0:
-        e = launch_bucket<kBucket[0].cl, kBucket[0].all, kBucket[0].nodal>(ms, b, a, q, queue, sq);
-        break;
-      case 1:
-        e = launch_bucket<kBucket[1].cl, kBucket[1].all, kBucket[1].nodal>(ms, b, a, q, queue, sq);
-        break;
-      case 2:
-        e = launch_bucket<kBucket[2].cl, kBucket[2].all, kBucket[2].nodal>(ms, b, a, q, queue, sq);
-        break;
-      case 3:
-        e = launch_bucket<kBucket[3].cl, kBucket[3].all, kBucket[3].nodal>(ms, b, a, q, queue, sq);
-        break;
-      case 4:
-        e = launch_bucket<kBucket[4].cl, kBucket[4].all, kBucket[4].nodal>(ms, b, a, q, queue, sq);
-        break;
-      default:
-        e = launch_bucket<kBucket[5].cl, kBucket[5].all, kBucket[5].nodal>(ms, b, a, q, queue, sq);
-        break;
-    }
+    e = with_bucket(q, [&](auto Q) {
+      return launch_bucket<decltype(Q)::value>(ms, b, a, queue, sq);
+    });
     if (e != cudaSuccess) return e;
     ++*launches;
     if ((e = cudaEventRecord(c.join[q], sq)) != cudaSuccess) return e;

@@ -221,3 +221,31 @@ def test_graph_replay_and_recapture(M):
                      stream=stream.cuda_stream)
         torch.cuda.synchronize()
         np.testing.assert_array_equal(sig_dev.cpu().numpy(), outs[0])
+
+
+def test_paired_small_rves_match_one_per_cta(M):
+    """Small RVEs (whole state within half a CTA's shared memory) are solved
+    two per CTA, each by a 512-thread group with its own named barrier; the
+    group reductions keep the order of a whole CTA, so the stresses,
+    displacements, step counts and statuses are those of one RVE per CTA, in
+    RAMP and in RELAX mode."""
+    from mumfim_gb300 import synthetic as S
+    w = S.config2(n_rve=24, steps=700, n_min=500, n_max=2_500)
+    for strat in (w.strategies,
+                  [M.SolutionStrategy(visc_damp_coeff=2.0, residual_tol=1e-7, max_steps=2_000)]
+                  * w.n_rve):
+        out = []
+        for per_cta in (2, 1):
+            g = M.BatchedFiberRVEAnalysisExplicit(w.networks, strat, precision="mixed",
+                                                  small_rves_per_cta=per_cta)
+            s = np.zeros((w.n_rve, 6))
+            g.run(w.F, s)
+            out.append((s, g.last_status.copy(), [g.displacements(r) for r in (0, 5, 23)]))
+            g.close()
+        (s2, st2, u2), (s1, st1, u1) = out
+        np.testing.assert_array_equal(s2, s1)
+        np.testing.assert_array_equal(st2["steps"], st1["steps"])
+        np.testing.assert_array_equal(st2["status"], st1["status"])
+        np.testing.assert_array_equal(st2["residual"], st1["residual"])
+        for a, b in zip(u2, u1):
+            np.testing.assert_array_equal(a, b)
