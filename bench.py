@@ -37,6 +37,12 @@ divided by wall time; RVE solves/s is reported beside it.
             (a model: the state stays on chip); roofline_binding gives the
             resource that does bind, the L1TEX (shared memory) pipe and the
             issue slots, from the committed ncu captures
+  autotune  before the timed runs the launch-shape tuner times 200-step
+            solves of 1024 RVEs of the batch (stratified by size) under
+            every candidate shape -- largest cluster, clusters of 4 instead
+            of 2, one or two small RVEs per CTA -- and the batch runs the
+            fastest (config.autotune holds the table; every shape gives the
+            same bits)
   cpu_baseline  the CPU oracle (a restatement of the reference's batched
             path: the reference itself needs Kokkos, PUMI, AMSI and MPI and
             cannot be built), its optimised timing build, on all host cores,
@@ -457,9 +463,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small-rves-per-cta", type=int, default=0,
                     help="mixed: small RVEs solved side by side per CTA (1 or 2; 0 = 2)")
-    ap.add_argument("--autotune", action="store_true",
-                    help="mixed: time 100-step solves under each cluster-size limit first and "
-                         "use the fastest (mumfim_gb300.autotune)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="mixed: skip the launch-shape tuner (mumfim_gb300.autotune) and use "
+                         "the default shape")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the FP64 side-by-side, the served streams and config 3")
     args = ap.parse_args()
@@ -488,18 +494,19 @@ def main():
 
     w, desc = build_workload(args.config, rank, args.n_rve, args.solve_steps, args.nodes)
     tune = None
-    if args.autotune and args.precision == "mixed":
-        from mumfim_gb300.autotune import tune_cluster_limit
-        t_tune = time.perf_counter()
-        best, table = tune_cluster_limit(w.networks, w.strategies, w.F, steps=100,
-                                         device=local_rank)
-        tune = {"max_cluster_ctas": best, "seconds": round(time.perf_counter() - t_tune, 1),
-                "fiber_steps_per_s_by_limit": {str(k): v for k, v in table.items()}}
+    shape = {"small_rves_per_cta": args.small_rves_per_cta}
+    if args.precision == "mixed" and not args.no_autotune and not args.small_rves_per_cta:
+        import dataclasses
+
+        from mumfim_gb300.autotune import tune_launch_shape
+        best, rep = tune_launch_shape(w.networks, w.strategies, w.F, device=local_rank)
+        shape = best.kwargs()
+        tune = {"best": dataclasses.asdict(best), "from_cache": rep["from_cache"],
+                "seconds": rep["seconds"], "sample_rves": rep["sample_rves"],
+                "steps": rep["steps"], "table": rep["table"]}
     t0 = time.perf_counter()
     gpu = m.BatchedFiberRVEAnalysisExplicit(w.networks, w.strategies, precision=args.precision,
-                                            device=local_rank,
-                                            max_cluster_ctas=tune["max_cluster_ctas"] if tune else 0,
-                                            small_rves_per_cta=args.small_rves_per_cta)
+                                            device=local_rank, **shape)
     setup_s = time.perf_counter() - t0
     R = w.n_rve
     fiber_steps = w.total_fibers * w.steps

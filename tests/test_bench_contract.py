@@ -85,3 +85,21 @@ def test_reference_arm_maps_no_product_library():
     assert "oracle/_build/liboracle_fast.so" in maps
     assert "oracle/_build/libnetgen.so" in maps
     assert "mumfim_gb300/_lib" not in maps, maps
+
+
+def test_autotune_candidates_and_sample():
+    """The tuner's host logic: distinct candidate shapes, a sample that keeps
+    the size mix, and a cache key that depends on the size mix."""
+    from types import SimpleNamespace
+
+    from mumfim_gb300.autotune import candidate_shapes, stratified_sample, workload_key
+    shapes = candidate_shapes()
+    assert len(shapes) == len(set(shapes)) == 12
+    nets = [SimpleNamespace(n_nodes=n, n_fibers=3 * n,
+                            reactions=[SimpleNamespace(law=n % 2)]) for n in range(500, 5500, 5)]
+    ids = stratified_sample(nets, 100)
+    assert len(ids) == 100 and len(set(ids)) == 100
+    sizes = sorted(nets[i].n_nodes for i in ids)
+    assert sizes[0] < 600 and sizes[-1] > 5300
+    assert workload_key(nets) == workload_key(list(reversed(nets)))
+    assert workload_key(nets) != workload_key(nets[:300])
