@@ -37,7 +37,7 @@ divided by wall time; RVE solves/s is reported beside it.
             (a model: the state stays on chip); roofline_binding gives the
             resource that does bind, the L1TEX (shared memory) pipe and the
             issue slots, from the committed ncu captures
-  autotune  before the timed runs the launch-shape tuner times 200-step
+  autotune  before the timed runs the launch-shape tuner times 500-step
             solves of 1024 RVEs of the batch (stratified by size) under
             every candidate shape -- largest cluster, clusters of 4 instead
             of 2, one or two small RVEs per CTA -- and the batch runs the

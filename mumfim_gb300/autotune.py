@@ -126,7 +126,7 @@ def _rate(networks, strat, F, shape: LaunchShape, repeats: int, device: int) -> 
     return float(sum(n.n_fibers for n in networks)) * steps / (best_ms * 1e-3)
 
 
-def tune_launch_shape(networks: Sequence, strategies: Sequence, F, steps: int = 200,
+def tune_launch_shape(networks: Sequence, strategies: Sequence, F, steps: int = 500,
                       sample: int = 1024, repeats: int = 2, device: int = 0,
                       candidates: Optional[Sequence[LaunchShape]] = None,
                       use_cache: bool = True) -> Tuple[LaunchShape, dict]:
