@@ -364,6 +364,12 @@ typedef struct mfg_server_result {
 } mfg_server_result;
 
 void mfg_default_server_options(mfg_server_options* out);
+/* No counterpart in the reference (which keeps every RVE on the device).
+ * Estimated device memory, in bytes, of a batch or server of these n_rve
+ * networks in the given precision: the figure mfg_server_create() admits
+ * against its HBM budget, for a caller that pages RVEs in and out of the
+ * device (export/import) under a budget of its own. Host only. */
+double mfg_device_bytes_estimate(const mfg_network* nets, int32_t n_rve, int32_t precision);
 /* Registers n_rve RVEs (as mfg_batch_create) and starts serving. Returns
  * MFG_E_BUSY when the RVEs' device state would exceed the HBM budget. */
 mfg_status mfg_server_create(const mfg_network* nets, const mfg_strategy* strategies,

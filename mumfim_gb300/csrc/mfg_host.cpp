@@ -1369,6 +1369,16 @@ mfg_status mfg_server_create(const mfg_network* nets, const mfg_strategy* strate
   return MFG_OK;
 }
 
+double mfg_device_bytes_estimate(const mfg_network* nets, int32_t n_rve, int32_t precision) {
+  if (!nets || n_rve < 1) return 0.0;
+  int64_t nt = 0, et = 0;
+  for (int r = 0; r < n_rve; ++r) {
+    nt += std::max(nets[r].n_nodes, 0);
+    et += std::max(nets[r].n_fibers, 0);
+  }
+  return batch_bytes(nt, et, nt / 8, n_rve, precision == MFG_PREC_MIXED);
+}
+
 mfg_status mfg_server_submit(mfg_server* sv, int32_t rve, const double* F, int32_t update_coords,
                              int64_t* ticket) {
   return mfg_server_submit_ex(sv, rve, F, update_coords, 0, ticket);

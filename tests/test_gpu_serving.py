@@ -193,3 +193,39 @@ def test_served_stiffness_equals_batch_run_then_stiffness(lib_path, precision):
         np.testing.assert_array_equal(rec["sigma"], s_ref[r])
         np.testing.assert_array_equal(rec["C"], C_ref[r])
     assert plain["stiffness_status"][0] == -1 and not plain["C"][0].any()
+
+
+def test_paged_server_evicts_and_matches_all_resident(lib_path):
+    """Admission per request under a device-memory budget that holds two
+    pages of two RVEs out of four pages: every round of updating requests
+    evicts idle pages to host memory and re-admits saved ones, and every
+    stress is bit-identical to one server holding all eight RVEs."""
+    from mumfim_gb300 import synthetic as S
+    from mumfim_gb300.serving import PagedRVEServer, RVEServer
+    w = S.config2(n_rve=8, steps=400, n_min=400, n_max=3000)
+    rounds = [[np.eye(3) + (S.uniform(S.param_seed(30 + k, r), 9) * 0.02 - 0.01).reshape(3, 3)
+               for r in range(w.n_rve)] for k in range(3)]
+
+    def run(sv):
+        out = []
+        for Fk in rounds:
+            for r in range(w.n_rve):
+                sv.submit(r, Fk[r], update_coords=True)
+            res = sv.drain()
+            assert len(res) == w.n_rve and (res["status"] == 0).all()
+            s = np.zeros((w.n_rve, 6))
+            s[res["rve"]] = res["sigma"]
+            out.append(s)
+        return out
+
+    with RVEServer(w.networks, w.strategies, precision="mixed") as sv:
+        ref = run(sv)
+    from mumfim_gb300.serving import device_bytes_estimate
+    pages = [w.networks[i:i + 2] for i in range(0, 8, 2)]
+    budget = sum(sorted(device_bytes_estimate(p) for p in pages)[-2:]) * 1.001
+    with PagedRVEServer(w.networks, w.strategies, hbm_budget_bytes=budget, page_size=2) as pv:
+        got = run(pv)
+        assert pv.evictions >= 6 and pv.admissions >= 8
+        assert len(pv.resident) <= 2
+    for a, b in zip(ref, got):
+        np.testing.assert_array_equal(a, b)
