@@ -17,6 +17,9 @@ divided by wall time; RVE solves/s is reported beside it.
   f64_same_batch  the plain FP64 kernel and the mixed kernel on the same
             stratified subset of the batch (every 4th RVE): their throughput
             ratio and the mixed stress error against FP64
+  stiffness the FD material stiffness (six perturbed solves) on every 16th
+            RVE, mixed precision: the reference's sequential order against
+            all six solves in flight at once (the same bits in RAMP mode)
   served_config2  config 2 itself through the continuous-batching server:
             every RVE one request (its F, 5,000 steps), Poisson arrivals at
             80 % of the server's saturated throughput on the same requests;
@@ -266,6 +269,31 @@ def f64_same_batch(m, w, every: int):
     return summary, ids, sig["f64"]
 
 
+def stiffness_section(m, w, every: int):
+    """The FD material stiffness on every `every`-th RVE of the batch, mixed
+    precision, after an updating solve: the six perturbed solves one after
+    the other (the reference's order) and all six in flight at once. In RAMP
+    mode both give the same bits; the second of two stiffness calls is
+    timed (the first captures the launch graphs)."""
+    sub = w.subset(range(0, w.n_rve, every))
+    secs, C = {}, {}
+    for mode in ("sequential", "concurrent"):
+        g = m.BatchedFiberRVEAnalysisExplicit(sub.networks, sub.strategies, precision="mixed",
+                                              stiffness=mode)
+        g.run(sub.F, update_coords=True)
+        g.computeMaterialStiffness()
+        t0 = time.perf_counter()
+        C[mode] = g.computeMaterialStiffness()
+        secs[mode] = time.perf_counter() - t0
+        g.close()
+    fs = 6.0 * sub.total_fibers * sub.steps
+    return {"subset": f"every {every}th RVE ({sub.n_rve} RVEs), {sub.steps} ramp steps per solve",
+            "sequential_s": secs["sequential"], "concurrent_s": secs["concurrent"],
+            "concurrent_speedup": secs["sequential"] / secs["concurrent"],
+            "concurrent_fiber_steps_per_s": fs / secs["concurrent"],
+            "bit_identical": bool(np.array_equal(C["sequential"], C["concurrent"]))}
+
+
 def serve_stream(m, w, passes, update: bool, rate_frac: float = 0.8):
     """Runs `passes` (each a list of per-point F) through one server: first
     one saturation pass of the first pass's requests, all queued at once
@@ -418,6 +446,9 @@ def config3_section(m, every: int):
                           f"kernel's resident CTAs, so its rate is a lower bound -- "
                           f"f64_same_batch has the full-occupancy FP64 rate)",
             "sigma_rel_err_mixed_vs_f64": float(err.max()),
+            "sigma_rel_err_median": float(np.median(err)),
+            "rves_over_1e-5": int((err > 1e-5).sum()),
+            "worst_rve": int(ids[int(np.argmax(err))]),
             "near_toe_frac_mean": float(near.mean()),
             "err_by_near_toe_quartile": bins}
 
@@ -613,6 +644,8 @@ def main():
     if rank == 0 and world == 1 and not args.no_extras:
         summary, ids, s64 = f64_same_batch(m, w, args.f64_every)
         line["f64_same_batch"] = summary
+        if args.precision == "mixed":
+            line["stiffness"] = stiffness_section(m, w, 16)
         if args.config == 2 and args.precision == "mixed":
             line["served_config2"] = served_config2(m, w, ids, s64,
                                                     summary["f64_fiber_steps_per_s"])
