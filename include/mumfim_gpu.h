@@ -403,6 +403,18 @@ mfg_batch* mfg_server_batch(mfg_server* server);
 /* Stops the kernel (after the solves in flight), frees everything. */
 mfg_status mfg_server_destroy(mfg_server* server);
 
+/* ---- metrics ---------------------------------------------------------- */
+/* Structured log for a service loop (the reference has only its timing
+ * prints, MultiscaleRVEAnalysis.cc:241,283-286): with a file set, every
+ * mfg_batch_create, mfg_batch_run, mfg_batch_run_device,
+ * mfg_batch_material_stiffness and every mfg_server_poll that returned
+ * results or timed out appends one JSON object per line -- the call, its
+ * status and message, sizes, per-RVE status counts, step counts, the
+ * largest residual, fiber-steps and device / wall times. NULL or "" turns
+ * it off. The MFG_METRICS_LOG environment variable sets it at the first
+ * call when this function was never called. Process-wide, thread-safe. */
+mfg_status mfg_set_metrics_log(const char* path);
+
 /* ---- timing ----------------------------------------------------------- */
 /* Device time of the last run's relaxation kernel and of the whole run, in
  * milliseconds, from CUDA events recorded on the launching stream. Valid

@@ -94,8 +94,16 @@ def load_library(path: str | None = None):
     L.mfg_batch_last_timing.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.mfg_batch_last_launches.restype = i32
     L.mfg_batch_last_launches.argtypes = [vp]
+    L.mfg_set_metrics_log.restype = i32
+    L.mfg_set_metrics_log.argtypes = [C.c_char_p]
     _lib = L
     return L
+
+
+def set_metrics_log(path: str | None) -> None:
+    """mfg_set_metrics_log(): append one JSON line per C-ABI call (create,
+    run, stiffness, server poll) to `path`; None turns it off."""
+    load_library().mfg_set_metrics_log(path.encode() if path else None)
 
 
 def _check(status: int, allow=(MFG_OK,)):

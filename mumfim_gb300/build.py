@@ -34,6 +34,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # (source, kind, extra flags)
 SOURCES = [
     ("mfg_host.cpp", "cxx", []),
+    ("mfg_metrics.cpp", "cxx", []),
     ("mfg_coupling.cpp", "cxx", []),
     ("mfg_mixed_order.cpp", "cxx", []),
     ("mfg_relax_f64.cu", "cuda", ["--fmad=false"]),

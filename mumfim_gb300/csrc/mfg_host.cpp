@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include "mfg_internal.h"
+#include "mfg_metrics.h"
 #include "mfg_mixed.h"
 #include "mumfim_gpu.h"
 
@@ -466,8 +467,8 @@ void mfg_default_options(mfg_options* out) {
   out->precision = MFG_PREC_F64;
 }
 
-mfg_status mfg_batch_create(const mfg_network* nets, const mfg_strategy* strategies,
-                            int32_t n_rve, const mfg_options* options, mfg_batch** out) {
+static mfg_status batch_create_impl(const mfg_network* nets, const mfg_strategy* strategies,
+                                    int32_t n_rve, const mfg_options* options, mfg_batch** out) {
   mfg::Trace trace("mfg_batch_create");
   g_last_error.clear();
   if (!out) return fail(MFG_E_INVALID, "out is NULL");
@@ -697,8 +698,9 @@ int32_t mfg_batch_n_fibers(const mfg_batch* b, int32_t r) {
   return (b && r >= 0 && r < b->R) ? b->n_fibers[r] : -1;
 }
 
-mfg_status mfg_batch_run_device(mfg_batch* b, const double* F_dev, int32_t n_F, double* sigma_dev,
-                                int32_t update_coords, mfg_rve_status* status_dev, void* stream) {
+static mfg_status batch_run_device_impl(mfg_batch* b, const double* F_dev, int32_t n_F,
+                                        double* sigma_dev, int32_t update_coords,
+                                        mfg_rve_status* status_dev, void* stream) {
   mfg::Trace trace("mfg_batch_run_device");
   g_last_error.clear();
   if (!b || !F_dev || !sigma_dev) return fail(MFG_E_INVALID, "NULL argument");
@@ -761,8 +763,8 @@ mfg_status mfg_batch_run_device_noalloc(mfg_batch* b, const double* F_dev, int32
   return MFG_OK;
 }
 
-mfg_status mfg_batch_run(mfg_batch* b, const double* F, int32_t n_F, double* sigma,
-                         int32_t update_coords, mfg_rve_status* status) {
+static mfg_status batch_run_impl(mfg_batch* b, const double* F, int32_t n_F, double* sigma,
+                                 int32_t update_coords, mfg_rve_status* status) {
   mfg::Trace trace("mfg_batch_run");
   g_last_error.clear();
   if (!b || !F || !sigma) return fail(MFG_E_INVALID, "NULL argument");
@@ -907,7 +909,7 @@ mfg_status stiffness_concurrent(mfg_batch* b, const double Fa[kStiffSlots][9], d
 
 extern "C" {
 
-mfg_status mfg_batch_material_stiffness(mfg_batch* b, double* C) {
+static mfg_status material_stiffness_impl(mfg_batch* b, double* C) {
   mfg::Trace trace("mfg_batch_material_stiffness");
   g_last_error.clear();
   if (!b || !C) return fail(MFG_E_INVALID, "NULL argument");
@@ -1410,8 +1412,8 @@ mfg_status mfg_server_submit_ex(mfg_server* sv, int32_t rve, const double* F,
   return server_ensure_running(sv);
 }
 
-mfg_status mfg_server_poll(mfg_server* sv, mfg_server_result* out, int32_t capacity,
-                           int32_t* n_out, int32_t timeout_ms) {
+static mfg_status server_poll_impl(mfg_server* sv, mfg_server_result* out, int32_t capacity,
+                                   int32_t* n_out, int32_t timeout_ms) {
   g_last_error.clear();
   if (!sv || !n_out || (capacity > 0 && !out)) return fail(MFG_E_INVALID, "NULL argument");
   *n_out = 0;
@@ -1478,6 +1480,181 @@ mfg_status mfg_server_destroy(mfg_server* sv) {
   mfg::Trace trace("mfg_server_destroy");
   delete sv;
   return MFG_OK;
+}
+
+}  // extern "C"
+
+// ============================================================================
+// Metrics records (mfg_metrics.cpp): one JSON line per outermost call.
+// ============================================================================
+namespace {
+
+thread_local int g_metrics_depth = 0;
+
+struct MetricsScope {
+  bool top;
+  MetricsScope() : top(g_metrics_depth++ == 0) {}
+  ~MetricsScope() { --g_metrics_depth; }
+  bool log() const { return top && mfg::metrics_enabled(); }
+};
+
+const char* precision_name(int p) { return p == MFG_PREC_MIXED ? "mixed" : "f64"; }
+
+std::string status_fields(const char* call, mfg_status st) {
+  char buf[256];
+  std::snprintf(buf, sizeof(buf), "\"call\": \"%s\", \"status\": \"%s\"", call,
+                mfg_status_string(st));
+  std::string o = buf;
+  if (st != MFG_OK && !g_last_error.empty())
+    o += ", \"message\": \"" + mfg::json_escape(g_last_error.c_str()) + "\"";
+  return o;
+}
+
+// Device times of the last run from the batch's events (completed runs only).
+void event_times(mfg_batch* b, float* relax_ms, float* run_ms) {
+  *relax_ms = -1.f;
+  *run_ms = -1.f;
+  if (!b || !b->timing_valid) return;
+  if (cudaEventSynchronize(b->ev_run1) != cudaSuccess) return;
+  if (cudaEventElapsedTime(relax_ms, b->ev_relax0, b->ev_relax1) != cudaSuccess) *relax_ms = -1.f;
+  if (cudaEventElapsedTime(run_ms, b->ev_run0, b->ev_run1) != cudaSuccess) *run_ms = -1.f;
+}
+
+}  // namespace
+
+extern "C" {
+
+mfg_status mfg_batch_create(const mfg_network* nets, const mfg_strategy* strategies,
+                            int32_t n_rve, const mfg_options* options, mfg_batch** out) {
+  MetricsScope ms;
+  const double t0 = mfg::wall_seconds();
+  const mfg_status st = batch_create_impl(nets, strategies, n_rve, options, out);
+  if (ms.log()) {
+    std::string f = status_fields("mfg_batch_create", st);
+    char buf[256];
+    std::snprintf(buf, sizeof(buf), ", \"n_rve\": %d, \"precision\": \"%s\", \"setup_ms\": %.3f",
+                  n_rve, precision_name(options ? options->precision : MFG_PREC_F64),
+                  1e3 * (mfg::wall_seconds() - t0));
+    f += buf;
+    if (st == MFG_OK && out && *out) {
+      std::snprintf(buf, sizeof(buf), ", \"nodes\": %lld, \"fibers\": %lld, \"device\": %d",
+                    static_cast<long long>((*out)->nt), static_cast<long long>((*out)->et),
+                    (*out)->device);
+      f += buf;
+    }
+    mfg::metrics_write(f);
+  }
+  return st;
+}
+
+mfg_status mfg_batch_run(mfg_batch* b, const double* F, int32_t n_F, double* sigma,
+                         int32_t update_coords, mfg_rve_status* status) {
+  MetricsScope ms;
+  if (!ms.log()) return batch_run_impl(b, F, n_F, sigma, update_coords, status);
+  const double t0 = mfg::wall_seconds();
+  std::vector<mfg_rve_status> tmp;
+  mfg_rve_status* st_out = status;
+  if (!st_out && b && b->R > 0) {
+    tmp.resize(b->R);
+    st_out = tmp.data();
+  }
+  const mfg_status st = batch_run_impl(b, F, n_F, sigma, update_coords, st_out);
+  const double wall_ms = 1e3 * (mfg::wall_seconds() - t0);
+  std::string f = status_fields("mfg_batch_run", st);
+  char buf[512];
+  if (b && st_out && st != MFG_E_INVALID && st != MFG_E_CUDA && st != MFG_E_OOM) {
+    int counts[9] = {};
+    long long smin = -1, smax = 0;
+    double ssum = 0, rmax = 0, fs = 0;
+    for (int r = 0; r < b->R; ++r) {
+      const mfg_rve_status& x = st_out[r];
+      if (x.status >= 0 && x.status < 9) counts[x.status]++;
+      smin = smin < 0 ? x.steps : std::min<long long>(smin, x.steps);
+      smax = std::max<long long>(smax, x.steps);
+      ssum += x.steps;
+      if (std::isfinite(x.residual)) rmax = std::max(rmax, x.residual);
+      fs += static_cast<double>(b->n_fibers[r]) * x.steps;
+    }
+    float relax_ms, run_ms;
+    event_times(b, &relax_ms, &run_ms);
+    std::snprintf(buf, sizeof(buf),
+                  ", \"n_rve\": %d, \"precision\": \"%s\", \"update_coords\": %d, \"n_F\": %d, "
+                  "\"ok\": %d, \"not_converged\": %d, \"nonfinite\": %d, \"steps_min\": %lld, "
+                  "\"steps_max\": %lld, \"steps_mean\": %.1f, \"residual_max\": %.6e, "
+                  "\"fiber_steps\": %.6e, \"relax_ms\": %.3f, \"run_ms\": %.3f, "
+                  "\"wall_ms\": %.3f, \"launches\": %d",
+                  b->R, precision_name(b->precision), update_coords ? 1 : 0, n_F, counts[MFG_OK],
+                  counts[MFG_E_NOT_CONVERGED], counts[MFG_E_NONFINITE], smin, smax,
+                  ssum / std::max(1, b->R), rmax, fs, relax_ms, run_ms, wall_ms, b->last_launches);
+    f += buf;
+  }
+  mfg::metrics_write(f);
+  return st;
+}
+
+mfg_status mfg_batch_run_device(mfg_batch* b, const double* F_dev, int32_t n_F, double* sigma_dev,
+                                int32_t update_coords, mfg_rve_status* status_dev, void* stream) {
+  MetricsScope ms;
+  const mfg_status st =
+      batch_run_device_impl(b, F_dev, n_F, sigma_dev, update_coords, status_dev, stream);
+  if (ms.log()) {
+    // enqueued, not completed: no per-RVE figures (they are on the device)
+    std::string f = status_fields("mfg_batch_run_device", st);
+    char buf[160];
+    std::snprintf(buf, sizeof(buf), ", \"n_rve\": %d, \"update_coords\": %d, \"launches\": %d",
+                  b ? b->R : 0, update_coords ? 1 : 0, b ? b->last_launches : 0);
+    f += buf;
+    mfg::metrics_write(f);
+  }
+  return st;
+}
+
+mfg_status mfg_batch_material_stiffness(mfg_batch* b, double* C) {
+  MetricsScope ms;
+  const double t0 = mfg::wall_seconds();
+  const mfg_status st = material_stiffness_impl(b, C);
+  if (ms.log()) {
+    std::string f = status_fields("mfg_batch_material_stiffness", st);
+    if (b) {
+      const bool conc = b->stiffness == MFG_STIFFNESS_CONCURRENT ||
+                        (b->stiffness == MFG_STIFFNESS_AUTO && b->all_ramp);
+      char buf[200];
+      std::snprintf(buf, sizeof(buf),
+                    ", \"n_rve\": %d, \"precision\": \"%s\", \"solves\": \"%s\", \"wall_ms\": %.3f",
+                    b->R, precision_name(b->precision), conc ? "concurrent" : "sequential",
+                    1e3 * (mfg::wall_seconds() - t0));
+      f += buf;
+    }
+    mfg::metrics_write(f);
+  }
+  return st;
+}
+
+mfg_status mfg_server_poll(mfg_server* sv, mfg_server_result* out, int32_t capacity,
+                           int32_t* n_out, int32_t timeout_ms) {
+  MetricsScope ms;
+  const mfg_status st = server_poll_impl(sv, out, capacity, n_out, timeout_ms);
+  const int n = n_out ? *n_out : 0;
+  if (ms.log() && (n > 0 || st != MFG_OK)) {
+    std::string f = status_fields("mfg_server_poll", st);
+    double lmax = 0, lsum = 0, dmax = 0;
+    int bad = 0;
+    for (int i = 0; i < n; ++i) {
+      lmax = std::max(lmax, out[i].latency_s);
+      lsum += out[i].latency_s;
+      dmax = std::max(dmax, out[i].device_s);
+      bad += out[i].status != MFG_OK;
+    }
+    char buf[256];
+    std::snprintf(buf, sizeof(buf),
+                  ", \"results\": %d, \"not_ok\": %d, \"latency_ms_mean\": %.3f, "
+                  "\"latency_ms_max\": %.3f, \"device_ms_max\": %.3f, \"outstanding\": %lld",
+                  n, bad, n ? 1e3 * lsum / n : 0.0, 1e3 * lmax, 1e3 * dmax,
+                  static_cast<long long>(sv ? sv->in_flight() : 0));
+    f += buf;
+    mfg::metrics_write(f);
+  }
+  return st;
 }
 
 }  // extern "C"
