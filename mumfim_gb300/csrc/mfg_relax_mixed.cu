@@ -104,7 +104,7 @@ struct MixedState {
   // incidence the other end's code and the fiber's data (solve_rve_nodal).
   int2* nsell = nullptr;         // nt
   int64_t* sell_off = nullptr;   // n_rve
-  int32_t* ncode = nullptr;      // SELL elements
+  int32_t* ncode = nullptr;      // set-up only: SELL element codes, packed into nfc
   float4* nfc = nullptr;         // SELL elements
   int64_t n_sell = 0;
   int64_t* nfib_tmp = nullptr;   // set-up only: fiber of each SELL element
@@ -164,6 +164,18 @@ __global__ void mixed_prepare_order_kernel(const DevBatch b, MixedState ms) {
   if (i < b.nt) ms.mmass[i] = ms.mass[ms.gnode[i]];
 }
 
+// 1 / l0 of a fiber from its FP32 reference difference. Every solve takes
+// 1 / l0 from this one expression -- the fiber-centric ones from the value
+// the set-up stores, the node-centric one by recomputing it from the dX it
+// loads -- so a fiber's force vector is the same bits in every solve.
+__device__ __forceinline__ float inv_length(float dx, float dy, float dz) {
+  const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+  const float r = rsqrtf(s);
+  // one Newton step, r (1 + (1 - s r^2) / 2): the approximate reciprocal
+  // square root to about half an ulp
+  return fmaf(r * 0.5f, fmaf(-s * r, r, 1.f), r);
+}
+
 __global__ void mixed_prepare_fibers_kernel(const DevBatch b, MixedState ms) {
   for (int rve = blockIdx.y; rve < b.n_rve; rve += gridDim.y) {
     const RveDesc d = b.desc[rve];
@@ -176,29 +188,31 @@ __global__ void mixed_prepare_fibers_kernel(const DevBatch b, MixedState ms) {
       const double* X = b.X + k * b.nt + no;
       dx[k] = static_cast<float>(X[c.y] - X[c.x]);
     }
-    ms.fcon[fo] = make_float4(dx[0], dx[1], dx[2], static_cast<float>(1.0 / b.l0[fo]));
+    ms.fcon[fo] = make_float4(dx[0], dx[1], dx[2], inv_length(dx[0], dx[1], dx[2]));
     ms.fconc[d.fiber_off + ms.mslot[fo]] = ms.fcon[fo];
   }
 }
 
-// Fiber data of the node-centric incidences (fiber -1: padding), oriented
-// from the other end to the incidence's node: X[n2] - X[n1] at the fiber's
-// second end, its negation at the first. The set-up codes carry the end in
-// bit 0; the solve needs only the other end's node code, so it is shifted
-// out here.
-__global__ void mixed_prepare_sell_kernel(const MixedState ms, const int64_t* nfib, int64_t n) {
+// Node-centric incidence records (fiber -1: padding): the fiber's reference
+// difference oriented from the other end to the incidence's node (X[n2] -
+// X[n1] at the fiber's second end, its negation at the first) and, in the
+// fourth word, the other end's node code (the set-up codes carry the end in
+// bit 0, which is shifted out). One 16-byte load per incidence; 1 / l0 is
+// recomputed from dX (inv_length).
+__global__ void mixed_prepare_sell_kernel(const MixedState ms, const int32_t* ncode,
+                                          const int64_t* nfib, int64_t n) {
   const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   if (i < n) {
     const int64_t e = nfib[i];
-    const int code = ms.ncode[i];
+    const int code = ncode[i];
     float4 fc = e >= 0 ? ms.fcon[e] : make_float4(0.f, 0.f, 0.f, 0.f);
     if (!(code & 1)) {
       fc.x = -fc.x;
       fc.y = -fc.y;
       fc.z = -fc.z;
     }
-    ms.nfc[i] = fc;
-    ms.ncode[i] = code >> 1;
+    reinterpret_cast<int4*>(ms.nfc)[i] =
+        make_int4(__float_as_int(fc.x), __float_as_int(fc.y), __float_as_int(fc.z), code >> 1);
   }
 }
 
@@ -924,22 +938,22 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
 // traffic is the end records plus the own state, against records, force
 // vector stores and force vector gathers in the fiber-centric solve above.
 // The vector of a fiber is the same bits at either end and as the fiber
-// pass forms it: the displacement difference is formed in the node's
-// direction and its sign flipped at the fiber's first end, which is exact
-// (rounding to nearest is symmetric), so both solves give the same results.
+// pass forms it (below), so both solves give the same results.
 //
 // Incidences are stored sliced by warp (SELL-32): the own nodes of a CTA, in
 // the order its threads visit them (free nodes, then boundary nodes), form
 // slices of 32, a slice as wide as its largest degree, and the k-th
 // incidence of the node at lane l of a slice is at slice base + 32 k + l. A
-// warp's loads of incidence codes and fiber data are then contiguous. An
-// incidence holds the other end's node code and the fiber's (X_me - X_o,
-// 1 / l0): its reference difference oriented from the other end to this
-// node (mixed_prepare_sell_kernel).
+// warp's loads of incidence records are then contiguous. An incidence is
+// one 16-byte record: the fiber's reference difference oriented from the
+// other end to this node, X_me - X_o, and the other end's node code
+// (mixed_prepare_sell_kernel); 1 / l0 is recomputed from the difference
+// with the expression the fiber-centric solves' stored value comes from
+// (inv_length), which a negation leaves unchanged.
 //
 // With both differences taken from the other end to this node, the vector
 // (dX + du) T / l is the fiber's force vector at its second end and exactly
-// its negation at the first: the TwoSum difference of the negated operands
+// its negation at the first: the rounded difference of the negated operands
 // is the negated difference (rounding to nearest is symmetric), the Green
 // strain is unchanged under (dX, du) -> (-dX, -du), and so is T / l. Adding
 // it is the same rounding as subtracting the second-end vector, so the sums
@@ -948,23 +962,23 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
 // Internal force of one node with record `me` from its deg incidences
 // starting at p.
 template <class Nodes>
-__device__ __forceinline__ void nodal_force(const Law& L, const Nodes& u, const int32_t* ncode,
-                                            const float4* nfc, int p, int deg, const NodeRec& me,
-                                            float& a0, float& a1, float& a2) {
+__device__ __forceinline__ void nodal_force(const Law& L, const Nodes& u, const float4* nfc, int p,
+                                            int deg, const NodeRec& me, float& a0, float& a1,
+                                            float& a2) {
   a0 = 0.f; a1 = 0.f; a2 = 0.f;
   if (deg <= 0) return;
-  int c = __ldg(ncode + p);
-  float4 fc = __ldg(nfc + p);
+  const int4* rec = reinterpret_cast<const int4*>(nfc);
+  int4 q = __ldg(rec + p);
   for (int k = 1;; ++k) {
     const bool more = k < deg;
-    int cn = c;
-    float4 fcn = fc;
+    int4 qn = q;
     if (more) {
       p += 32;
-      cn = __ldg(ncode + p);
-      fcn = __ldg(nfc + p);
+      qn = __ldg(rec + p);
     }
-    const NodeRec o = u.load(c);
+    const float dx = __int_as_float(q.x), dy = __int_as_float(q.y), dz = __int_as_float(q.z);
+    const float4 fc = make_float4(dx, dy, dz, inv_length(dx, dy, dz));
+    const NodeRec o = u.load(q.w);
     float du[3];
     disp_diff(o, me, du);  // x_me - x_o
     const float g = green(du, fc);
@@ -975,8 +989,7 @@ __device__ __forceinline__ void nodal_force(const Law& L, const Nodes& u, const 
     a1 = __fadd_rn(a1, f.y);
     a2 = __fadd_rn(a2, f.z);
     if (!more) break;
-    c = cn;
-    fc = fcn;
+    q = qn;
   }
 }
 
@@ -986,7 +999,7 @@ __device__ __forceinline__ void nodal_force(const Law& L, const Nodes& u, const 
 // kRes also returns this thread's share of the squared residual norm.
 template <bool kRes, class Nodes>
 __device__ __forceinline__ double nodal_kick(const Law& L, const Nodes& u, const LocalNodes& own,
-                                             float* vel, const int32_t* ncode, const float4* nfc,
+                                             float* vel, const float4* nfc,
                                              const int2* srow, const float2* mass, int nfo,
                                              float hk, float c) {
   double part = 0.0;
@@ -1004,7 +1017,7 @@ __device__ __forceinline__ double nodal_kick(const Law& L, const Nodes& u, const
       mmn = __ldg(mass + tn);
     }
     float f[3];
-    nodal_force(L, u, ncode, nfc, sr.x, sr.y, own.load(t), f[0], f[1], f[2]);
+    nodal_force(L, u, nfc, sr.x, sr.y, own.load(t), f[0], f[1], f[2]);
     if constexpr (kRes)
       part += static_cast<double>(f[0]) * f[0] + static_cast<double>(f[1]) * f[1] +
               static_cast<double>(f[2]) * f[2];
@@ -1085,7 +1098,6 @@ __device__ void solve_rve_nodal(const DevBatch& b, const MixedState& ms, const R
   r.ramp = reinterpret_cast<float*>(b.ramp + 6 * d.bnd_off);
   const int2* srow = ms.nsell + no;  // by node position: (first incidence, degree)
   const int64_t so = ms.sell_off[rve];
-  const int32_t* ncode = ms.ncode + so;
   const float4* nfc = ms.nfc + so;
   const float2* mass = ms.mmass + no;
   const double* F = a.F + 9 * (a.n_F > 1 ? rve : 0);
@@ -1122,8 +1134,8 @@ __device__ void solve_rve_nodal(const DevBatch& b, const MixedState& ms, const R
     // pass A (compiled apart for the residual steps, so that the FP64
     // residual sum costs nothing on the others)
     const double part =
-        res_step ? nodal_kick<true>(r.L, u, own, vel, ncode, nfc, srow + f_lo, mass + f_lo, nfo, hk, c)
-                 : nodal_kick<false>(r.L, u, own, vel, ncode, nfc, srow + f_lo, mass + f_lo, nfo, hk,
+        res_step ? nodal_kick<true>(r.L, u, own, vel, nfc, srow + f_lo, mass + f_lo, nfo, hk, c)
+                 : nodal_kick<false>(r.L, u, own, vel, nfc, srow + f_lo, mass + f_lo, nfo, hk,
                                      c);
     if (res_step) {
       residual = sqrt(Ops::template combine<false>(block_sum<kThreadsMixed>(part, red), cred));
@@ -1171,7 +1183,7 @@ __device__ void solve_rve_nodal(const DevBatch& b, const MixedState& ms, const R
     if (i >= NF) {
       const int2 sr = __ldg(srow + i);
       float a0, a1, a2;
-      nodal_force(r.L, u, ncode, nfc, sr.x, sr.y, nr, a0, a1, a2);
+      nodal_force(r.L, u, nfc, sr.x, sr.y, nr, a0, a1, a2);
       b.fint[no + i] = a0;
       b.fint[nt + no + i] = a1;
       b.fint[2 * nt + no + i] = a2;
@@ -1737,13 +1749,15 @@ cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<Rv
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ms.n_sell > 0) {
     mixed_prepare_sell_kernel<<<static_cast<unsigned>((ms.n_sell + 255) / 256), 256, 0, s>>>(
-        ms, ms.nfib_tmp, ms.n_sell);
+        ms, ms.ncode, ms.nfib_tmp, ms.n_sell);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   // the fiber ids were only needed to fill the incidences' fiber data
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
   cudaFree(ms.nfib_tmp);
   ms.nfib_tmp = nullptr;
+  cudaFree(ms.ncode);
+  ms.ncode = nullptr;
   return cudaSuccess;
 }
 
