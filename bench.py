@@ -492,8 +492,12 @@ def main():
     ap.add_argument("--serve-steps", type=int, default=500)
     ap.add_argument("--config3-every", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--small-rve-solve", choices=("auto", "node", "fiber"), default="auto",
+                    help="mixed: solve of the RVEs whose node state fits one CTA "
+                         "(auto = node-centric)")
     ap.add_argument("--small-rves-per-cta", type=int, default=0,
-                    help="mixed: small RVEs solved side by side per CTA (1 or 2; 0 = 2)")
+                    help="mixed, fiber-centric small solve: small RVEs side by side per CTA "
+                         "(1 or 2; 0 = 2)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="mixed: skip the launch-shape tuner (mumfim_gb300.autotune) and use "
                          "the default shape")
@@ -525,8 +529,9 @@ def main():
 
     w, desc = build_workload(args.config, rank, args.n_rve, args.solve_steps, args.nodes)
     tune = None
-    shape = {"small_rves_per_cta": args.small_rves_per_cta}
-    if args.precision == "mixed" and not args.no_autotune and not args.small_rves_per_cta:
+    shape = {"small_rves_per_cta": args.small_rves_per_cta, "small_rve_solve": args.small_rve_solve}
+    if (args.precision == "mixed" and not args.no_autotune and not args.small_rves_per_cta
+            and args.small_rve_solve == "auto"):
         import dataclasses
 
         from mumfim_gb300.autotune import tune_launch_shape

@@ -125,11 +125,28 @@ typedef struct mfg_options {
                                clusters; the results are the same either way. */
   int32_t stiffness;        /* mfg_stiffness_solves: how mfg_batch_material_stiffness()
                                runs its six perturbed solves */
-  int32_t small_rves_per_cta; /* mixed precision: how many small RVEs (whole state within
-                               half a CTA's shared memory) one CTA solves side by side,
-                               1 or 2 (0 = 2); the results are the same either way */
-  int32_t reserved[1];
+  int32_t small_rves_per_cta; /* mixed precision, MFG_SMALL_FIBER_CENTRIC only: how many
+                               small RVEs (whole state within half a CTA's shared
+                               memory) one CTA solves side by side, 1 or 2 (0 = 2);
+                               the results are the same either way */
+  int32_t small_rve_solve;  /* mixed precision: mfg_small_rve_solve */
 } mfg_options;
+
+/* Mixed precision: the solve of an RVE whose node state fits one CTA. Both
+ * give the same bits; only the speed differs.
+ *  NODE_CENTRIC   every incident fiber evaluated at each free node, node
+ *                 state in shared memory (the solve of the larger RVEs too).
+ *  FIBER_CENTRIC  a fiber pass stores each fiber's force vector, a node pass
+ *                 gathers them; the whole state in shared memory where it
+ *                 fits, two small RVEs per CTA by small_rves_per_cta.
+ *  AUTO           per RVE: NODE_CENTRIC on the linear law (faster on every
+ *                 size measured), FIBER_CENTRIC on the nonlinear law (whose
+ *                 exponential NODE_CENTRIC evaluates at both fiber ends). */
+typedef enum mfg_small_rve_solve {
+  MFG_SMALL_AUTO = 0,
+  MFG_SMALL_NODE_CENTRIC = 1,
+  MFG_SMALL_FIBER_CENTRIC = 2
+} mfg_small_rve_solve;
 
 /* The six perturbed solves of mfg_batch_material_stiffness(). The reference
  * runs them as six whole-batch runs one after the other

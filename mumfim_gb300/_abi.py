@@ -29,6 +29,7 @@ MFG_MODE_RAMP = 1
 MFG_PREC_F64 = 0
 MFG_PREC_MIXED = 1
 MFG_STIFFNESS = {"auto": 0, "sequential": 1, "concurrent": 2}
+MFG_SMALL_RVE_SOLVE = {"auto": 0, "node": 1, "fiber": 2}
 
 
 class mfg_reaction(C.Structure):
@@ -52,7 +53,7 @@ class mfg_options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("device", C.c_int32),
                 ("threads_per_rve", C.c_int32), ("max_cluster_ctas", C.c_int32),
                 ("cluster_layout", C.c_int32), ("stiffness", C.c_int32),
-                ("small_rves_per_cta", C.c_int32), ("reserved", C.c_int32 * 1)]
+                ("small_rves_per_cta", C.c_int32), ("small_rve_solve", C.c_int32)]
 
 
 class mfg_rve_status(C.Structure):

@@ -1,17 +1,20 @@
 """Launch-shape autotuner for the mixed-precision batch.
 
-The mixed solve places each RVE by rule: two small RVEs per CTA where their
-whole state fits half of its shared memory, else the smallest single CTA or
+The mixed solve places each RVE by rule: the smallest single CTA or
 thread-block cluster (2, 4, then 8 CTAs) whose shared memory holds the
-RVE's node state, else one CTA streaming from global memory. Which shapes
-pay depends on the GPU and on the size mix: a cluster trades barrier and
+RVE's node state (node-centric solve), else one CTA streaming from global
+memory; on request, RVEs whose whole state fits one CTA (or half of one,
+two per CTA) take the fiber-centric solve first. Which shapes pay depends
+on the GPU and on the size mix: a cluster trades barrier and
 distributed-shared-memory costs for on-chip state, how many clusters of a
-size stay resident varies, and pairing small RVEs trades a second RVE's
-share of the SM against a half-size CTA per RVE. The tuner times short
-solves of a size-stratified sample of the batch under every candidate shape
--- the largest cluster allowed (``max_cluster_ctas``), clusters of 4 instead
-of 2 (the serving layout) and one or two small RVEs per CTA -- and keeps the
-fastest. Every candidate gives the same bits, so only the speed differs.
+size stay resident varies, and the fiber-centric solve of small RVEs trades
+half the fiber arithmetic against a stored force vector per fiber and a
+second pass. The tuner times short solves of a size-stratified sample of
+the batch under every candidate shape -- the largest cluster allowed
+(``max_cluster_ctas``), clusters of 4 instead of 2 (the serving layout) and
+the solve of small RVEs (node-centric, or fiber-centric two per CTA) -- and
+keeps the fastest. Every candidate gives the same bits, so only the speed
+differs.
 
 Choices are cached per (GPU, SM count, size-mix histogram, law mix) in a
 JSON file (``MFG_AUTOTUNE_CACHE``, default ``mumfim_gb300/_lib/autotune.json``).
@@ -36,25 +39,37 @@ _PKG = os.path.dirname(os.path.abspath(__file__))
 class LaunchShape:
     max_cluster_ctas: int = 0     # 1, 2, 4 or 8 (0 = 8)
     serving_layout: bool = False  # clusters of 4 where the batch layout takes 2
-    small_rves_per_cta: int = 0   # 1 or 2 (0 = 2)
+    small_rves_per_cta: int = 0   # fiber-centric small solve: 1 or 2 (0 = 2)
+    small_rve_solve: str = "auto"  # "auto" (= "node"), "node" or "fiber"
 
     def kwargs(self) -> dict:
         return dict(max_cluster_ctas=self.max_cluster_ctas, serving_layout=self.serving_layout,
-                    small_rves_per_cta=self.small_rves_per_cta)
+                    small_rves_per_cta=self.small_rves_per_cta,
+                    small_rve_solve=self.small_rve_solve)
 
 
-DEFAULT_SHAPE = LaunchShape(8, False, 2)
+DEFAULT_SHAPE = LaunchShape(8, False, 0, "auto")
+CANDIDATES_VERSION = 3  # small solve: auto (by law), node- or fiber-centric
 
 
-def candidate_shapes() -> List[LaunchShape]:
+def candidate_shapes(nonlinear_frac: float = 0.0) -> List[LaunchShape]:
     """Every distinct shape: the serving layout only differs from the batch
-    layout when clusters of 4 are allowed."""
+    layout when clusters of 4 are allowed; the small solve "auto" (node-
+    centric on the linear law, fiber-centric on the nonlinear one) is tried
+    beside whichever of "node" and "fiber" differs from it on this law mix,
+    the fiber-centric one with two small RVEs per CTA (one per CTA measured
+    slower)."""
+    solves = [("auto", 2)]
+    if nonlinear_frac > 0.0:
+        solves.append(("node", 0))
+    if nonlinear_frac < 1.0:
+        solves.append(("fiber", 2))
     out = []
-    for per_cta in (2, 1):
+    for solve, per_cta in solves:
         for mc in (8, 4, 2, 1):
-            out.append(LaunchShape(mc, False, per_cta))
+            out.append(LaunchShape(mc, False, per_cta, solve))
             if mc >= 4:
-                out.append(LaunchShape(mc, True, per_cta))
+                out.append(LaunchShape(mc, True, per_cta, solve))
     return out
 
 
@@ -70,8 +85,9 @@ def stratified_sample(networks: Sequence, size: int) -> List[int]:
 
 def workload_key(networks: Sequence, device: int = 0) -> str:
     """Cache key: GPU name and SM count, the histogram of log2(node count) in
-    half-octave bins (fractions to 0.02), mean fibers per node, and the
-    fraction of RVEs on the nonlinear law."""
+    half-octave bins (fractions to 0.02), mean fibers per node, the
+    fraction of RVEs on the nonlinear law, and the version of the candidate
+    set (a choice among other candidates is not reused)."""
     try:
         import torch
         p = torch.cuda.get_device_properties(device)
@@ -85,8 +101,8 @@ def workload_key(networks: Sequence, device: int = 0) -> str:
     hist = {k: round(v, 2) for k, v in hist.items() if v > 0}
     fpn = round(float(sum(n.n_fibers for n in networks)) / float(nodes.sum()), 1)
     nl = round(float(np.mean([n.reactions[0].law == 1 for n in networks])), 1)
-    return json.dumps({"gpu": gpu, "hist": hist, "fibers_per_node": fpn, "nonlinear": nl},
-                      sort_keys=True)
+    return json.dumps({"gpu": gpu, "hist": hist, "fibers_per_node": fpn, "nonlinear": nl,
+                       "candidates": CANDIDATES_VERSION}, sort_keys=True)
 
 
 def _cache_path() -> str:
@@ -146,7 +162,8 @@ def tune_launch_shape(networks: Sequence, strategies: Sequence, F, steps: int = 
                                    strategies[r].crit_time_scale_factor) for r in ids]
     F = np.ascontiguousarray(F, dtype=np.float64).reshape(len(networks), 3, 3)[ids]
     table = []
-    for shape in (candidates or candidate_shapes()):
+    nl = float(np.mean([n.reactions[0].law == 1 for n in networks]))
+    for shape in (candidates or candidate_shapes(nl)):
         table.append({"shape": dataclasses.asdict(shape),
                       "fiber_steps_per_s": _rate(nets, strat, F, shape, repeats, device)})
     best = max(table, key=lambda t: t["fiber_steps_per_s"])

@@ -126,12 +126,15 @@ class BatchedFiberRVEAnalysisExplicit:
     stiffness   "auto", "sequential" or "concurrent": how computeMaterialStiffness
                 runs its six perturbed solves (mfg_stiffness_solves in
                 include/mumfim_gpu.h)
-    small_rves_per_cta  mixed precision: 1 or 2 small RVEs per CTA (0 = 2); same results
+    small_rve_solve  mixed precision: "auto" (= "node"), "node" or "fiber": the solve of
+                RVEs whose node state fits one CTA (mfg_small_rve_solve); same results
+    small_rves_per_cta  mixed precision, "fiber" only: 1 or 2 small RVEs per CTA (0 = 2)
     """
 
     def __init__(self, networks: Sequence, strategies: Sequence, precision: str = "f64",
                  device: int = 0, max_cluster_ctas: int = 0, serving_layout: bool = False,
-                 stiffness: str = "auto", small_rves_per_cta: int = 0):
+                 stiffness: str = "auto", small_rves_per_cta: int = 0,
+                 small_rve_solve: str = "auto"):
         L = load_library()
         if len(networks) != len(strategies):
             raise ValueError("There must be a solution strategy for each fiber network!")
@@ -143,6 +146,7 @@ class BatchedFiberRVEAnalysisExplicit:
         opts.cluster_layout = 1 if serving_layout else 0
         opts.stiffness = _abi.MFG_STIFFNESS[stiffness]
         opts.small_rves_per_cta = small_rves_per_cta
+        opts.small_rve_solve = _abi.MFG_SMALL_RVE_SOLVE[small_rve_solve]
         h = C.c_void_p()
         _check(L.mfg_batch_create(self._arr.nets, self._arr.strats, len(networks), C.byref(opts),
                                   C.byref(h)))

@@ -490,6 +490,10 @@ static mfg_status batch_create_impl(const mfg_network* nets, const mfg_strategy*
   if (opt.small_rves_per_cta < 0 || opt.small_rves_per_cta > 2)
     return fail(MFG_E_INVALID, "small_rves_per_cta must be 0, 1 or 2 (got %d)",
                 opt.small_rves_per_cta);
+  if (opt.small_rve_solve != MFG_SMALL_AUTO && opt.small_rve_solve != MFG_SMALL_NODE_CENTRIC &&
+      opt.small_rve_solve != MFG_SMALL_FIBER_CENTRIC)
+    return fail(MFG_E_INVALID, "small_rve_solve must be MFG_SMALL_AUTO, _NODE_CENTRIC or "
+                "_FIBER_CENTRIC (got %d)", opt.small_rve_solve);
   if (opt.stiffness != MFG_STIFFNESS_AUTO && opt.stiffness != MFG_STIFFNESS_SEQUENTIAL &&
       opt.stiffness != MFG_STIFFNESS_CONCURRENT)
     return fail(MFG_E_INVALID, "stiffness must be MFG_STIFFNESS_AUTO, _SEQUENTIAL or _CONCURRENT "
@@ -674,6 +678,7 @@ static mfg_status batch_create_impl(const mfg_network* nets, const mfg_strategy*
         b->mixed ? mfg::mixed_create(*b->mixed, dv, b->desc, conn, rowptr, inc, b->sms,
                                      opt.max_cluster_ctas > 0 ? opt.max_cluster_ctas : 8,
                                      opt.cluster_layout == MFG_LAYOUT_SERVING,
+                                     opt.small_rve_solve,
                                      opt.small_rves_per_cta > 0 ? opt.small_rves_per_cta : 2, s)
                  : cudaErrorMemoryAllocation;
     if (e != cudaSuccess)

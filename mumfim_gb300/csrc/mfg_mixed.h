@@ -24,12 +24,14 @@ constexpr int kMixedContexts = 7;
 // and CSR rows on the host (RVEs with an order of their own, and the
 // node-centric incidence blocks, are built from them). max_cluster bounds
 // the cluster size; serving_layout takes clusters of 4 where the batch
-// layout would take 2; rves_per_cta (1 or 2) bounds how many small RVEs
-// share a CTA.
+// layout would take 2. small_solve (mfg_small_rve_solve) picks the solve of
+// the RVEs whose node state fits one CTA; with the fiber-centric one, up to
+// rves_per_cta (1 or 2) small RVEs share a CTA.
 cudaError_t mixed_create(MixedState& ms, const DevBatch& b, const std::vector<RveDesc>& desc,
                          const std::vector<int2>& conn, const std::vector<int32_t>& rowptr,
                          const std::vector<int32_t>& inc, int sms, int max_cluster,
-                         bool serving_layout, int rves_per_cta, cudaStream_t s);
+                         bool serving_layout, int small_solve, int rves_per_cta,
+                         cudaStream_t s);
 // One run: reads the persistent FP64 state (x, u, vol), relaxes in mixed
 // precision and writes the FP64 state, stress and status back. `ctx` picks
 // the run context (0 for the batch's runs); runs on different contexts may

@@ -95,6 +95,9 @@ def test_autotune_candidates_and_sample():
     from mumfim_gb300.autotune import candidate_shapes, stratified_sample, workload_key
     shapes = candidate_shapes()
     assert len(shapes) == len(set(shapes)) == 12
+    assert {s.small_rve_solve for s in shapes} == {"auto", "fiber"}
+    assert {s.small_rve_solve for s in candidate_shapes(1.0)} == {"auto", "node"}
+    assert len(set(candidate_shapes(0.5))) == 18
     nets = [SimpleNamespace(n_nodes=n, n_fibers=3 * n,
                             reactions=[SimpleNamespace(law=n % 2)]) for n in range(500, 5500, 5)]
     ids = stratified_sample(nets, 100)

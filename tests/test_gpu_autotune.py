@@ -1,5 +1,5 @@
 """Launch-shape autotuner: it times candidate shapes (largest cluster,
-serving layout, small RVEs per CTA) on a size-stratified sample of the batch,
+serving layout, solve of small RVEs) on a size-stratified sample of the batch,
 picks the fastest and caches the choice per GPU and size mix; a shape changes
 speed, never results."""
 import numpy as np
@@ -14,7 +14,8 @@ def test_tune_launch_shape_and_cache(lib_path, tmp_path, monkeypatch):
     from mumfim_gb300.autotune import LaunchShape, tune_launch_shape
     monkeypatch.setenv("MFG_AUTOTUNE_CACHE", str(tmp_path / "cache.json"))
     w = S.config2(n_rve=24, steps=200, n_min=600, n_max=14_000)
-    cands = [LaunchShape(8, False, 2), LaunchShape(4, True, 1), LaunchShape(1, False, 2)]
+    cands = [LaunchShape(8, False, 0, "node"), LaunchShape(4, True, 1, "fiber"),
+             LaunchShape(1, False, 2, "fiber")]
     best, rep = tune_launch_shape(w.networks, w.strategies, w.F, steps=40, sample=16,
                                   repeats=1, candidates=cands)
     assert not rep["from_cache"] and rep["sample_rves"] == 16

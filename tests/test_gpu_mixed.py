@@ -26,8 +26,9 @@ def M(lib_path):
     return m
 
 
-def _solve(M, w, precision, **kw):
-    g = M.BatchedFiberRVEAnalysisExplicit(w.networks, w.strategies, precision=precision)
+def _solve(M, w, precision, opts=None, **kw):
+    g = M.BatchedFiberRVEAnalysisExplicit(w.networks, w.strategies, precision=precision,
+                                          **(opts or {}))
     sig = np.zeros((w.n_rve, 6))
     g.run(w.F, sig, **kw)
     return g, sig
@@ -92,11 +93,12 @@ def test_mixed_incremental_and_transactional_runs(M):
 
 
 def test_mixed_every_placement_and_cluster_size(M):
-    """One RVE per way a batch run places an RVE: fiber-centric with all
-    mutable state in one CTA's shared memory (800 nodes), node-centric on one
-    CTA (4,000) and over clusters of 2, 4 and 8 CTAs (9,000 / 20,000 /
-    40,000), fiber-centric in global memory (80,000). Each agrees with FP64,
-    and each gives the same bits solved alone as in the mixed-size batch."""
+    """One RVE per way a batch run places an RVE: node-centric on one CTA
+    (800 and 4,000 nodes) and over clusters of 2, 4 and 8 CTAs (9,000 /
+    20,000 / 40,000), fiber-centric in global memory (80,000), and on
+    request fiber-centric with all mutable state in one CTA's shared memory
+    (800, 4,000). Each agrees with FP64, and each gives the same bits solved
+    alone as in the mixed-size batch, whichever solve."""
     from mumfim_gb300 import synthetic as S
     sizes = (800, 4_000, 9_000, 20_000, 40_000, 80_000)
     nets, F = [], []
@@ -111,12 +113,19 @@ def test_mixed_every_placement_and_cluster_size(M):
     g64, s64 = _solve(M, w, "f64")
     g32, s32 = _solve(M, w, "mixed")
     assert (g32.last_status["steps"] == 1_000).all()
+    # one launch per non-empty size bucket -- node-centric on one CTA (800,
+    # 4,000), clusters of 2, 4 and 8, the run-time placement -- and the
+    # status pack
+    assert g32.last_launches() == 5 + 1
     for r in range(len(sizes)):
         assert _rel(s32[r], s64[r]) <= REL_MIXED, r
     for r in (0, 2, 4, 5):
         one = w.subset([r])
         _, s1 = _solve(M, one, "mixed")
         np.testing.assert_array_equal(s1[0], s32[r])
+    gf, sf = _solve(M, w.subset([0, 1]), "mixed", {"small_rve_solve": "fiber"})
+    assert gf.last_launches() == 2 + 1  # fiber-centric pair (800), node-centric (4,000)
+    np.testing.assert_array_equal(sf, s32[:2])
 
 
 def test_cluster_and_single_cta_solves_agree(M):
@@ -224,10 +233,11 @@ def test_graph_replay_and_recapture(M):
 
 
 def test_paired_small_rves_match_one_per_cta(M):
-    """Small RVEs (whole state within half a CTA's shared memory) are solved
-    two per CTA, each by a 512-thread group with its own named barrier; the
-    group reductions keep the order of a whole CTA, so the stresses,
-    displacements, step counts and statuses are those of one RVE per CTA, in
+    """With the fiber-centric small solve, small RVEs (whole state within
+    half a CTA's shared memory) are solved two per CTA, each by a 512-thread
+    group with its own named barrier; the group reductions keep the order of
+    a whole CTA, so the stresses, displacements, step counts and statuses
+    are those of one RVE per CTA, and those of the node-centric solve, in
     RAMP and in RELAX mode."""
     from mumfim_gb300 import synthetic as S
     w = S.config2(n_rve=24, steps=700, n_min=500, n_max=2_500)
@@ -235,17 +245,22 @@ def test_paired_small_rves_match_one_per_cta(M):
                   [M.SolutionStrategy(visc_damp_coeff=2.0, residual_tol=1e-7, max_steps=2_000)]
                   * w.n_rve):
         out = []
-        for per_cta in (2, 1):
+        for solve, per_cta in (("fiber", 2), ("fiber", 1), ("node", 0)):
             g = M.BatchedFiberRVEAnalysisExplicit(w.networks, strat, precision="mixed",
+                                                  small_rve_solve=solve,
                                                   small_rves_per_cta=per_cta)
             s = np.zeros((w.n_rve, 6))
             g.run(w.F, s)
             out.append((s, g.last_status.copy(), [g.displacements(r) for r in (0, 5, 23)]))
             g.close()
-        (s2, st2, u2), (s1, st1, u1) = out
-        np.testing.assert_array_equal(s2, s1)
-        np.testing.assert_array_equal(st2["steps"], st1["steps"])
-        np.testing.assert_array_equal(st2["status"], st1["status"])
-        np.testing.assert_array_equal(st2["residual"], st1["residual"])
-        for a, b in zip(u2, u1):
-            np.testing.assert_array_equal(a, b)
+        s2, st2, u2 = out[0]
+        for k, (s1, st1, u1) in enumerate(out[1:]):
+            np.testing.assert_array_equal(s2, s1)
+            np.testing.assert_array_equal(st2["steps"], st1["steps"])
+            np.testing.assert_array_equal(st2["status"], st1["status"])
+            if k == 0:  # the pair's group sums keep a whole CTA's order
+                np.testing.assert_array_equal(st2["residual"], st1["residual"])
+            else:  # the node-centric order sums the residual in another order
+                np.testing.assert_allclose(st2["residual"], st1["residual"], rtol=1e-9)
+            for a, b in zip(u2, u1):
+                np.testing.assert_array_equal(a, b)
