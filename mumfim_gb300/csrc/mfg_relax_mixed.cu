@@ -63,7 +63,7 @@ namespace mfg {
 // arguments, and the run-time placement's global scratch. Context 0 serves
 // the batch's runs; contexts 1-6 the concurrent perturbed solves of the
 // material stiffness, which run at the same time on the same batch.
-constexpr int kMixedBuckets = 7;
+constexpr int kMixedBuckets = 8;
 struct MixedRunCtx {
   int32_t* queues = nullptr;  // one claim counter per bucket (device)
   float* u_hl = nullptr;      // run-time placement scratch; null: the batch's own
@@ -138,18 +138,20 @@ struct BucketKind {
   bool all;    // fiber-centric: force vectors in shared memory too
   bool nodal;  // node-centric solve (node state in shared memory)
   int ng;      // RVEs solved side by side by one CTA (fiber-centric, all on chip)
+  bool db;     // node-centric on one CTA with two copies of the node records
 };
 constexpr int kBuckets = kMixedBuckets;
-constexpr BucketKind kBucket[kBuckets] = {{8, false, true, 1}, {4, false, true, 1},
-                                          {2, false, true, 1}, {1, false, true, 1},
-                                          {1, true, false, 1}, {1, true, false, 2},
-                                          {1, false, false, 1}};
+constexpr BucketKind kBucket[kBuckets] = {
+    {8, false, true, 1, false}, {4, false, true, 1, false}, {2, false, true, 1, false},
+    {1, false, true, 1, false}, {1, false, true, 1, true},  {1, true, false, 1, false},
+    {1, true, false, 2, false}, {1, false, false, 1, false}};
 // Placement preference (bucket_of): the first bucket whose shared memory
 // holds the RVE, else the last bucket.
-constexpr int kPref[] = {5, 4, 3, 2, 1, 0};
+constexpr int kPref[] = {6, 5, 4, 3, 2, 1, 0};
 // The single-CTA buckets with an RVE order of their own, by kind.
-constexpr int kQNodal1 = 3, kQFiberAll = 4, kQFiberPair = 5;
+constexpr int kQNodal1 = 3, kQNodalDB = 4, kQFiberAll = 5, kQFiberPair = 6;
 static_assert(kBucket[kQNodal1].cl == 1 && kBucket[kQNodal1].nodal, "bucket table");
+static_assert(kBucket[kQNodalDB].cl == 1 && kBucket[kQNodalDB].db, "bucket table");
 static_assert(kBucket[kQFiberAll].cl == 1 && kBucket[kQFiberAll].all, "bucket table");
 static_assert(kBucket[kQFiberPair].all && kBucket[kQFiberPair].ng == 2, "bucket table");
 
@@ -656,14 +658,15 @@ __device__ __forceinline__ void mixed_stress(const DevBatch& b, const RunArgs& a
 
 // Shared-memory floats per CTA of an RVE solved by CL CTAs: 9 per node slot
 // (displacement hi, lo and velocity; ceil(NF/CL) free plus ceil(NB/CL)
-// boundary slots), plus 4 per fiber slot (ceil(E/CL)) when the force vectors
-// are kept in shared memory too (all: the fiber-centric single CTA).
+// boundary slots), 15 with two copies of the node records, plus 4 per fiber
+// slot (ceil(E/CL)) when the force vectors are kept in shared memory too
+// (all: the fiber-centric single CTA).
 __host__ __device__ inline int64_t cluster_floats(int n_nodes, int n_free, int n_fibers, int cl,
-                                                  bool all) {
+                                                  bool all, bool two_copies = false) {
   const int64_t nb = n_nodes - n_free;
   const int64_t cap = (static_cast<int64_t>(n_free) + cl - 1) / cl + (nb + cl - 1) / cl;
   const int64_t echunk = (static_cast<int64_t>(n_fibers) + cl - 1) / cl;
-  return 9 * cap + (all ? 4 * echunk : 0);
+  return (two_copies ? 15 : 9) * cap + (all ? 4 * echunk : 0);
 }
 
 // Prologue of a solve in FP64 for the CTA's own nodes: the affine predictor
@@ -727,12 +730,12 @@ __device__ __forceinline__ void mixed_prologue(const DevBatch& b, const MixedSta
 // RAMP mode: the own boundary nodes move by their exact (hi, lo) increment.
 template <int NG = 1>
 __device__ __forceinline__ void ramp_boundary(const Rve& r, const LocalNodes& own, int g_lo,
-                                              int g_hi, int fchunk) {
+                                              int g_hi, int fchunk, const LocalNodes* dst = nullptr) {
   const int NF = r.d.n_free;
   for (int i = g_lo + Group<NG>::tid(); i < g_hi; i += Group<NG>::kSize) {
     const float* rb = r.ramp + 12 * (i - NF);
-    float* rec = own.rec(fchunk + (i - g_lo));
-    NodeRec nr = load_rec(rec);
+    const int li = fchunk + (i - g_lo);
+    NodeRec nr = load_rec(own.rec(li));
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       float s, e;
@@ -740,7 +743,7 @@ __device__ __forceinline__ void ramp_boundary(const Rve& r, const LocalNodes& ow
       nr.hi[k] = s;
       nr.lo[k] = nr.lo[k] + (e + rb[3 + k]);
     }
-    store_rec(rec, nr);
+    store_rec((dst ? *dst : own).rec(li), nr);  // in place, or into the other copy
   }
 }
 
@@ -999,11 +1002,15 @@ __device__ __forceinline__ void nodal_force(const Law& L, const Nodes& u, const 
 // of the CTA's own free nodes t = tid, tid + kThreadsMixed, ... < nfo, the
 // next node's row and mass loaded while the current one is summed. With
 // kRes also returns this thread's share of the squared residual norm.
-template <bool kRes, class Nodes>
+// With kFuse (two copies of the node records) the same thread then drifts
+// the node at once, x += 2 h v with the new v, into the other copy `nxt`:
+// the arithmetic of pass B, without its barrier.
+template <bool kRes, bool kFuse = false, class Nodes>
 __device__ __forceinline__ double nodal_kick(const Law& L, const Nodes& u, const LocalNodes& own,
                                              float* vel, const float4* nfc,
                                              const int2* srow, const float2* mass, int nfo,
-                                             float hk, float c) {
+                                             float hk, float c, const LocalNodes* nxt = nullptr,
+                                             float h2 = 0.f) {
   double part = 0.0;
   int t = threadIdx.x;
   if (t >= nfo) return part;
@@ -1019,17 +1026,26 @@ __device__ __forceinline__ double nodal_kick(const Law& L, const Nodes& u, const
       mmn = __ldg(mass + tn);
     }
     float f[3];
-    nodal_force(L, u, nfc, sr.x, sr.y, own.load(t), f[0], f[1], f[2]);
+    const NodeRec me = own.load(t);
+    nodal_force(L, u, nfc, sr.x, sr.y, me, f[0], f[1], f[2]);
     if constexpr (kRes)
       part += static_cast<double>(f[0]) * f[0] + static_cast<double>(f[1]) * f[1] +
               static_cast<double>(f[2]) * f[2];
     const float mc = mm.y * c;
     const float km = hk * mm.x;
+    float wn[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       float w = vel[3 * t + k];
       w = fmaf(km, -f[k] - mc * w, w);
       vel[3 * t + k] = w;
+      wn[k] = w;
+    }
+    if constexpr (kFuse) {
+      NodeRec nr = me;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) comp_add(nr.hi[k], nr.lo[k], h2 * wn[k]);
+      store_rec(nxt->rec(t), nr);
     }
     if (!more) break;
     t = tn;
@@ -1064,9 +1080,10 @@ __device__ __forceinline__ float length_pass(const Rve& r, const Nodes& u, int e
 // each own free node's force, sums the residual on those steps and applies
 // the kick (v += h f / m, both half kicks in one); pass B, after a barrier,
 // drifts the own free nodes (x += 2h v) and moves the RAMP boundary.
-template <int CL>
+template <int CL, bool kDB = false>
 __device__ void solve_rve_nodal(const DevBatch& b, const MixedState& ms, const RunArgs& a, int rve,
                                 double* red, double* cred, float* smem) {
+  static_assert(!kDB || CL == 1, "two record copies on one CTA only");
   using Ops = ClusterOps<CL>;
   Rve r;
   r.d = b.desc[rve];
@@ -1090,7 +1107,11 @@ __device__ void solve_rve_nodal(const DevBatch& b, const MixedState& ms, const R
   Nodes u;         // every node of the RVE
   LocalNodes own;  // the node records this CTA updates, by local index
   own.hl = smem;
-  float* vel = smem + 6 * cap;
+  // kDB: a second copy of the records, which each step drifts into; the two
+  // copies swap roles every step
+  LocalNodes nxt;
+  nxt.hl = smem + 6 * cap;
+  float* vel = smem + (kDB ? 12 : 6) * cap;
   if constexpr (CL > 1)
     u.base = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
   else
@@ -1110,6 +1131,12 @@ __device__ void solve_rve_nodal(const DevBatch& b, const MixedState& ms, const R
   if (a.update_coords && rank == 0 && tid == 0) b.vol[rve] = jacobian(Fm) * b.vol[rve];
   mixed_prologue<true>(b, ms, r, Fm, ramp, f_lo, g_lo, nfo, n_own, fchunk, own, vel);
   Ops::sync();
+  if constexpr (kDB) {
+    // boundary records in the second copy too (RAMP moves them into it every
+    // step; RELAX never moves them); read there only after a step's barrier
+    for (int t = tid; t < g_hi - g_lo; t += kThreadsMixed)
+      store_rec(nxt.rec(fchunk + t), load_rec(own.rec(fchunk + t)));
+  }
   double dt_crit = Ops::template combine<true>(
                        block_min<kThreadsMixed>(length_pass(r, u, e_lo, e_hi), red), cred) /
                    d.sound_speed;
@@ -1133,37 +1160,48 @@ __device__ void solve_rve_nodal(const DevBatch& b, const MixedState& ms, const R
     }
     const float h = h_cur;
     const float hk = h_prev + h;  // trailing kick of step-1 + leading kick of step
+    const float h2 = h + h;
     // pass A (compiled apart for the residual steps, so that the FP64
-    // residual sum costs nothing on the others)
+    // residual sum costs nothing on the others); with two record copies
+    // pass B is fused into it and writes the other copy
     const double part =
-        res_step ? nodal_kick<true>(r.L, u, own, vel, nfc, srow + f_lo, mass + f_lo, nfo, hk, c)
-                 : nodal_kick<false>(r.L, u, own, vel, nfc, srow + f_lo, mass + f_lo, nfo, hk,
-                                     c);
+        res_step ? nodal_kick<true, kDB>(r.L, u, own, vel, nfc, srow + f_lo, mass + f_lo, nfo, hk,
+                                         c, &nxt, h2)
+                 : nodal_kick<false, kDB>(r.L, u, own, vel, nfc, srow + f_lo, mass + f_lo, nfo,
+                                          hk, c, &nxt, h2);
     if (res_step) {
       residual = sqrt(Ops::template combine<false>(block_sum<kThreadsMixed>(part, red), cred));
+      // a break keeps the copy of the step's start: the drift is dropped
       if (!isfinite(residual)) {
         status = 4;
         break;
       }
       if (!ramp && !(residual > d.tol)) break;
       if (step >= step_cap) break;
-    } else {
+    } else if constexpr (!kDB) {
       Ops::sync();
     }
-    // pass B: drift
-    const float h2 = h + h;
-    for (int t = tid; t < nfo; t += kThreadsMixed) {
-      float* rec = own.rec(t);
-      NodeRec nr = load_rec(rec);
+    if constexpr (!kDB) {
+      // pass B: drift
+      for (int t = tid; t < nfo; t += kThreadsMixed) {
+        float* rec = own.rec(t);
+        NodeRec nr = load_rec(rec);
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const float w = vel[3 * t + k];
-        comp_add(nr.hi[k], nr.lo[k], h2 * w);
+        for (int k = 0; k < 3; ++k) {
+          const float w = vel[3 * t + k];
+          comp_add(nr.hi[k], nr.lo[k], h2 * w);
+        }
+        store_rec(rec, nr);
       }
-      store_rec(rec, nr);
     }
-    if (ramp) ramp_boundary(r, own, g_lo, g_hi, fchunk);
+    if (ramp) ramp_boundary(r, own, g_lo, g_hi, fchunk, kDB ? &nxt : nullptr);
     Ops::sync();
+    if constexpr (kDB) {
+      const LocalNodes t = own;
+      own = nxt;
+      nxt = t;
+      u = own;
+    }
     h_prev = h;
     ++step;
   }
@@ -1200,12 +1238,13 @@ __device__ void solve_rve_nodal(const DevBatch& b, const MixedState& ms, const R
 // takes the next RVE of `order` (largest first) until the bucket is empty.
 // With NG = 2 each half of the CTA is a group that takes RVEs on its own,
 // in half of the shared memory, synchronised by its own named barrier.
-template <int CL, bool kAll, bool kNodal, int NG>
+template <int CL, bool kAll, bool kNodal, int NG, bool kDB>
 __global__ void __launch_bounds__(kThreadsMixed, 1)
 relax_mixed_kernel(const DevBatch b, const MixedState ms, const RunArgs a, int smem_floats,
                    const int32_t* order, int n_order, int32_t* queue) {
   static_assert(kNodal || CL == 1, "the fiber-centric solve runs on one CTA");
   static_assert(NG == 1 || (CL == 1 && kAll && !kNodal), "only small fiber-centric RVEs pair up");
+  static_assert(!kDB || (CL == 1 && kNodal), "two record copies: node-centric, one CTA");
   constexpr int kRed = kThreadsMixed / 32 + 1;
   extern __shared__ float4 smem4[];
   float* smem = reinterpret_cast<float*>(smem4);
@@ -1231,7 +1270,7 @@ relax_mixed_kernel(const DevBatch b, const MixedState ms, const RunArgs a, int s
     }
     if (rve < 0) break;
     if constexpr (kNodal)
-      solve_rve_nodal<CL>(b, ms, a, rve, red, cred, smem);
+      solve_rve_nodal<CL, kDB>(b, ms, a, rve, red, cred, smem);
     else
       solve_rve_mixed<kAll, NG>(b, ms, a, rve, red + g * kRed, smem + g * (smem_floats / NG),
                                 smem_floats / NG);
@@ -1247,6 +1286,8 @@ __device__ __forceinline__ void serve_one_cta(const DevBatch& b, const MixedStat
   const int q = __ldg(ms.rve_bucket + rve);
   if (q == kQNodal1)
     solve_rve_nodal<1>(b, ms, a, rve, red, cred, smem);
+  else if (q == kQNodalDB)
+    solve_rve_nodal<1, true>(b, ms, a, rve, red, cred, smem);
   else if (q == kQFiberAll || q == kQFiberPair)
     solve_rve_mixed<true>(b, ms, a, rve, red, smem, smem_floats);
   else
@@ -1522,7 +1563,8 @@ int bucket_of(const RveDesc& d, int smem_floats, int max_cluster, bool serving_l
     if ((fiber_small || !kBucket[q].all) && kBucket[q].cl <= max_cluster &&
         !(serving_layout && kBucket[q].cl == 2) && kBucket[q].ng <= rves_per_cta &&
         cluster_floats(d.n_nodes, d.n_free, d.n_fibers, kBucket[q].cl,
-                       kBucket[q].all && !kBucket[q].nodal) <= smem_floats / kBucket[q].ng)
+                       kBucket[q].all && !kBucket[q].nodal, kBucket[q].db) <=
+            smem_floats / kBucket[q].ng)
       return q;
   return kBuckets - 1;
 }
@@ -1538,10 +1580,11 @@ cudaError_t with_bucket(int q, Fn&& fn) {
     case 4: return fn(std::integral_constant<int, 4>{});
     case 5: return fn(std::integral_constant<int, 5>{});
     case 6: return fn(std::integral_constant<int, 6>{});
+    case 7: return fn(std::integral_constant<int, 7>{});
     default: return cudaErrorInvalidValue;
   }
 }
-static_assert(kBuckets == 7, "with_bucket covers every bucket");
+static_assert(kBuckets == 8, "with_bucket covers every bucket");
 
 template <int CL, bool kAll>
 cudaLaunchConfig_t launch_config(const MixedState& ms, unsigned grid, cudaStream_t s,
@@ -1568,7 +1611,7 @@ cudaError_t launch_bucket(const MixedState& ms, const DevBatch& b, const RunArgs
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg =
       launch_config<k.cl, k.all>(ms, static_cast<unsigned>(ms.bucket_grid[Q]), s, attr);
-  return cudaLaunchKernelEx(&cfg, relax_mixed_kernel<k.cl, k.all, k.nodal, k.ng>, b, ms, a,
+  return cudaLaunchKernelEx(&cfg, relax_mixed_kernel<k.cl, k.all, k.nodal, k.ng, k.db>, b, ms, a,
                             static_cast<int>(ms.smem_bytes / sizeof(float)),
                             static_cast<const int32_t*>(ms.order + ms.bucket_off[Q]), n, queue);
 }
@@ -1576,7 +1619,7 @@ cudaError_t launch_bucket(const MixedState& ms, const DevBatch& b, const RunArgs
 template <int Q>
 cudaError_t setup_bucket(MixedState& ms, int n) {
   constexpr BucketKind k = kBucket[Q];
-  cudaError_t e = cudaFuncSetAttribute(relax_mixed_kernel<k.cl, k.all, k.nodal, k.ng>,
+  cudaError_t e = cudaFuncSetAttribute(relax_mixed_kernel<k.cl, k.all, k.nodal, k.ng, k.db>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        ms.smem_bytes);
   if (e != cudaSuccess) return e;
@@ -1587,7 +1630,7 @@ cudaError_t setup_bucket(MixedState& ms, int n) {
         launch_config<k.cl, k.all>(ms, static_cast<unsigned>(k.cl * ms.sms), nullptr, attr);
     clusters = 0;
     if ((e = cudaOccupancyMaxActiveClusters(&clusters,
-                                            relax_mixed_kernel<k.cl, k.all, k.nodal, k.ng>,
+                                            relax_mixed_kernel<k.cl, k.all, k.nodal, k.ng, k.db>,
                                             &cfg)) != cudaSuccess)
       return e;
     if (clusters < 1) return cudaErrorInvalidConfiguration;

@@ -94,8 +94,9 @@ def test_mixed_incremental_and_transactional_runs(M):
 
 def test_mixed_every_placement_and_cluster_size(M):
     """One RVE per way a batch run places an RVE: node-centric on one CTA
-    (800 and 4,000 nodes) and over clusters of 2, 4 and 8 CTAs (9,000 /
-    20,000 / 40,000), fiber-centric in global memory (80,000), and on
+    with two copies of the node records (800 nodes) and with one (4,000),
+    over clusters of 2, 4 and 8 CTAs (9,000 / 20,000 / 40,000),
+    fiber-centric in global memory (80,000), and on
     request fiber-centric with all mutable state in one CTA's shared memory
     (800, 4,000). Each agrees with FP64, and each gives the same bits solved
     alone as in the mixed-size batch, whichever solve."""
@@ -113,10 +114,10 @@ def test_mixed_every_placement_and_cluster_size(M):
     g64, s64 = _solve(M, w, "f64")
     g32, s32 = _solve(M, w, "mixed")
     assert (g32.last_status["steps"] == 1_000).all()
-    # one launch per non-empty size bucket -- node-centric on one CTA (800,
-    # 4,000), clusters of 2, 4 and 8, the run-time placement -- and the
-    # status pack
-    assert g32.last_launches() == 5 + 1
+    # one launch per non-empty size bucket -- node-centric on one CTA with two
+    # record copies (800) and one (4,000), clusters of 2, 4 and 8, the
+    # run-time placement -- and the status pack
+    assert g32.last_launches() == 6 + 1
     for r in range(len(sizes)):
         assert _rel(s32[r], s64[r]) <= REL_MIXED, r
     for r in (0, 2, 4, 5):
