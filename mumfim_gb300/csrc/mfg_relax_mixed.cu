@@ -30,9 +30,10 @@
 //
 // Placement: one CTA of 1024 threads per SM with 220 KB of dynamic shared
 // memory, in size buckets launched concurrently. RVEs run node-centric on
-// one CTA or on the 2, 4 or 8 CTAs of a thread-block cluster, each CTA
-// keeping its nodes' records (hi, lo) and velocities in shared memory and
-// reading other CTAs' through distributed shared memory; on request, RVEs
+// one CTA (small ones with two copies of their node records, so the drift
+// fuses into the kick) or on the 2, 4 or 8 CTAs of a thread-block cluster,
+// each CTA keeping its nodes' records (hi, lo) and velocities in shared
+// memory and reading other CTAs' through distributed shared memory; on request, RVEs
 // whose whole state fits one CTA's shared memory (or half of it, two per
 // CTA) run fiber-centric instead.
 // Those RVEs get their own fiber and node order (cluster_order) that keeps
