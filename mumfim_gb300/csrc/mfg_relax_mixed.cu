@@ -64,7 +64,7 @@ namespace mfg {
 // arguments, and the run-time placement's global scratch. Context 0 serves
 // the batch's runs; contexts 1-6 the concurrent perturbed solves of the
 // material stiffness, which run at the same time on the same batch.
-constexpr int kMixedBuckets = 8;
+constexpr int kMixedBuckets = 10;
 struct MixedRunCtx {
   int32_t* queues = nullptr;  // one claim counter per bucket (device)
   float* u_hl = nullptr;      // run-time placement scratch; null: the batch's own
@@ -143,14 +143,16 @@ struct BucketKind {
 };
 constexpr int kBuckets = kMixedBuckets;
 constexpr BucketKind kBucket[kBuckets] = {
-    {8, false, true, 1, false}, {4, false, true, 1, false}, {2, false, true, 1, false},
-    {1, false, true, 1, false}, {1, false, true, 1, true},  {1, true, false, 1, false},
-    {1, true, false, 2, false}, {1, false, false, 1, false}};
+    {8, false, true, 1, false}, {4, false, true, 1, true},   {4, false, true, 1, false},
+    {2, false, true, 1, true},  {2, false, true, 1, false},  {1, false, true, 1, false},
+    {1, false, true, 1, true},  {1, true, false, 1, false},  {1, true, false, 2, false},
+    {1, false, false, 1, false}};
 // Placement preference (bucket_of): the first bucket whose shared memory
-// holds the RVE, else the last bucket.
-constexpr int kPref[] = {6, 5, 4, 3, 2, 1, 0};
+// holds the RVE, else the last bucket. At each cluster size two copies of
+// the node records come first where they fit.
+constexpr int kPref[] = {8, 7, 6, 5, 3, 4, 1, 2, 0};
 // The single-CTA buckets with an RVE order of their own, by kind.
-constexpr int kQNodal1 = 3, kQNodalDB = 4, kQFiberAll = 5, kQFiberPair = 6;
+constexpr int kQNodal1 = 5, kQNodalDB = 6, kQFiberAll = 7, kQFiberPair = 8;
 static_assert(kBucket[kQNodal1].cl == 1 && kBucket[kQNodal1].nodal, "bucket table");
 static_assert(kBucket[kQNodalDB].cl == 1 && kBucket[kQNodalDB].db, "bucket table");
 static_assert(kBucket[kQFiberAll].cl == 1 && kBucket[kQFiberAll].all, "bucket table");
@@ -1084,7 +1086,6 @@ __device__ __forceinline__ float length_pass(const Rve& r, const Nodes& u, int e
 template <int CL, bool kDB = false>
 __device__ void solve_rve_nodal(const DevBatch& b, const MixedState& ms, const RunArgs& a, int rve,
                                 double* red, double* cred, float* smem) {
-  static_assert(!kDB || CL == 1, "two record copies on one CTA only");
   using Ops = ClusterOps<CL>;
   Rve r;
   r.d = b.desc[rve];
@@ -1201,7 +1202,10 @@ __device__ void solve_rve_nodal(const DevBatch& b, const MixedState& ms, const R
       const LocalNodes t = own;
       own = nxt;
       nxt = t;
-      u = own;
+      if constexpr (CL > 1)
+        u.base = static_cast<uint32_t>(__cvta_generic_to_shared(own.hl));
+      else
+        u = own;
     }
     h_prev = h;
     ++step;
@@ -1245,7 +1249,7 @@ relax_mixed_kernel(const DevBatch b, const MixedState ms, const RunArgs a, int s
                    const int32_t* order, int n_order, int32_t* queue) {
   static_assert(kNodal || CL == 1, "the fiber-centric solve runs on one CTA");
   static_assert(NG == 1 || (CL == 1 && kAll && !kNodal), "only small fiber-centric RVEs pair up");
-  static_assert(!kDB || (CL == 1 && kNodal), "two record copies: node-centric, one CTA");
+  static_assert(!kDB || kNodal, "two record copies: node-centric solve");
   constexpr int kRed = kThreadsMixed / 32 + 1;
   extern __shared__ float4 smem4[];
   float* smem = reinterpret_cast<float*>(smem4);
@@ -1582,10 +1586,12 @@ cudaError_t with_bucket(int q, Fn&& fn) {
     case 5: return fn(std::integral_constant<int, 5>{});
     case 6: return fn(std::integral_constant<int, 6>{});
     case 7: return fn(std::integral_constant<int, 7>{});
+    case 8: return fn(std::integral_constant<int, 8>{});
+    case 9: return fn(std::integral_constant<int, 9>{});
     default: return cudaErrorInvalidValue;
   }
 }
-static_assert(kBuckets == 8, "with_bucket covers every bucket");
+static_assert(kBuckets == 10, "with_bucket covers every bucket");
 
 template <int CL, bool kAll>
 cudaLaunchConfig_t launch_config(const MixedState& ms, unsigned grid, cudaStream_t s,

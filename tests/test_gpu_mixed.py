@@ -93,15 +93,16 @@ def test_mixed_incremental_and_transactional_runs(M):
 
 
 def test_mixed_every_placement_and_cluster_size(M):
-    """One RVE per way a batch run places an RVE: node-centric on one CTA
-    with two copies of the node records (800 nodes) and with one (4,000),
-    over clusters of 2, 4 and 8 CTAs (9,000 / 20,000 / 40,000),
-    fiber-centric in global memory (80,000), and on
+    """One RVE per way a batch run places an RVE: node-centric with two
+    copies of the node records on one CTA (800 nodes) and over clusters of
+    2 and 4 CTAs (7,000 / 14,000), with one copy on one CTA (4,000) and over
+    clusters of 2, 4 and 8 CTAs (9,000 / 20,000 / 40,000), fiber-centric in
+    global memory (80,000), and on
     request fiber-centric with all mutable state in one CTA's shared memory
     (800, 4,000). Each agrees with FP64, and each gives the same bits solved
     alone as in the mixed-size batch, whichever solve."""
     from mumfim_gb300 import synthetic as S
-    sizes = (800, 4_000, 9_000, 20_000, 40_000, 80_000)
+    sizes = (800, 4_000, 9_000, 20_000, 40_000, 80_000, 7_000, 14_000)
     nets, F = [], []
     for i, n in enumerate(sizes):
         coords, conn = S.knn_network(n, 4, S.geometry_seed(7, i))
@@ -114,13 +115,13 @@ def test_mixed_every_placement_and_cluster_size(M):
     g64, s64 = _solve(M, w, "f64")
     g32, s32 = _solve(M, w, "mixed")
     assert (g32.last_status["steps"] == 1_000).all()
-    # one launch per non-empty size bucket -- node-centric on one CTA with two
-    # record copies (800) and one (4,000), clusters of 2, 4 and 8, the
+    # one launch per non-empty size bucket -- node-centric with two record
+    # copies on 1, 2 and 4 CTAs, with one on 1, 2, 4 and 8 CTAs, the
     # run-time placement -- and the status pack
-    assert g32.last_launches() == 6 + 1
+    assert g32.last_launches() == 8 + 1
     for r in range(len(sizes)):
         assert _rel(s32[r], s64[r]) <= REL_MIXED, r
-    for r in (0, 2, 4, 5):
+    for r in (0, 2, 4, 5, 6, 7):
         one = w.subset([r])
         _, s1 = _solve(M, one, "mixed")
         np.testing.assert_array_equal(s1[0], s32[r])
@@ -131,14 +132,15 @@ def test_mixed_every_placement_and_cluster_size(M):
 
 def test_cluster_and_single_cta_solves_agree(M):
     """The same RVEs solved node-centric over thread-block clusters (1, 2, 4
-    and 8 CTAs), in the serving layout (clusters of 4 instead of 2) and on
+    and 8 CTAs, with one or two copies of the node records), in the serving
+    layout (clusters of 4 instead of 2) and on
     one CTA each (max_cluster_ctas=1: node-centric where the node state
     fits, else fiber-centric with run-time placement): the same per-fiber
     and per-node arithmetic in the same order, so the same bits, in RAMP
     mode and in RELAX mode (there the step count too; only the residual's
     last bits may differ, since a cluster sums it in per-CTA parts)."""
     from mumfim_gb300 import synthetic as S
-    sizes = (4_000, 9_000, 20_000, 40_000)
+    sizes = (4_000, 9_000, 20_000, 40_000, 7_000, 14_000)
     nets, F = [], []
     for i, n in enumerate(sizes):
         coords, conn = S.knn_network(n, 4, S.geometry_seed(11, i))
