@@ -30,12 +30,13 @@
 //
 // Placement: one CTA of 1024 threads per SM with 220 KB of dynamic shared
 // memory, in size buckets launched concurrently. RVEs run node-centric on
-// one CTA (small ones with two copies of their node records, so the drift
-// fuses into the kick) or on the 2, 4 or 8 CTAs of a thread-block cluster,
-// each CTA keeping its nodes' records (hi, lo) and velocities in shared
-// memory and reading other CTAs' through distributed shared memory; on request, RVEs
-// whose whole state fits one CTA's shared memory (or half of it, two per
-// CTA) run fiber-centric instead.
+// one CTA or on the 2, 4 or 8 CTAs of a thread-block cluster, each CTA
+// keeping its nodes' records (hi, lo) and velocities in shared memory and
+// reading other CTAs' through distributed shared memory; where a second copy
+// of the records fits at that size, the drift fuses into the kick and a
+// step has one barrier instead of two. On the nonlinear law, or on request,
+// RVEs whose whole state fits one CTA's shared memory (or half of it, two
+// per CTA) run fiber-centric instead.
 // Those RVEs get their own fiber and node order (cluster_order) that keeps
 // most loads local and the warps' work even. RVEs too large for a cluster of
 // 8 run fiber-centric on one CTA, placed by size at run time down to global
@@ -1543,7 +1544,8 @@ void mixed_destroy(MixedState* ms) {
 namespace {
 
 // Bucket of an RVE: the smallest of one CTA or a cluster of 2, 4 or 8 CTAs
-// whose shared memory holds its node state (node-centric solve), else one
+// whose shared memory holds its node state (node-centric solve; at that
+// size with two copies of the node records where they fit), else one
 // CTA that keeps what fits in shared memory and streams the rest from global
 // memory (fiber-centric solve). Clusters of 8 are the last resort: with
 // 220 KB per CTA only 15 of them (120 SMs) are resident at once, against 36
