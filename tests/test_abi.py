@@ -105,7 +105,8 @@ def test_valid_input_without_gpu_reports_no_device(lib_path):
 
 @pytest.mark.parametrize("field,value,msg", [
     ("max_cluster_ctas", 3, "max_cluster_ctas"), ("cluster_layout", 7, "cluster_layout"),
-    ("precision", 5, "precision"),
+    ("precision", 5, "precision"), ("stiffness", 3, "stiffness"),
+    ("small_rves_per_cta", 3, "small_rves_per_cta"), ("small_rve_solve", 3, "small_rve_solve"),
 ])
 def test_bad_options_are_rejected_before_the_device(lib_path, field, value, msg):
     """Option checks come before any device call, so they hold on a machine
