@@ -317,48 +317,62 @@ __device__ __forceinline__ uint32_t cluster_addr(uint32_t local, uint32_t o) {
   return remote;
 }
 
-// A node record: displacement hi x, y, z then lo x, y, z, six floats read
-// and written as three 8-byte pairs.
+// A node record: displacement hi x, y, z and lo x, y, z.
 struct NodeRec {
   float hi[3], lo[3];
 };
-__device__ __forceinline__ NodeRec load_rec(const float* rec) {
-  const float2* p = reinterpret_cast<const float2*>(rec);
-  const float2 a = p[0], b = p[1], c = p[2];
-  return {{a.x, a.y, b.x}, {b.y, c.x, c.y}};
-}
-__device__ __forceinline__ void store_rec(float* rec, const NodeRec& r) {
-  float2* p = reinterpret_cast<float2*>(rec);
-  p[0] = make_float2(r.hi[0], r.hi[1]);
-  p[1] = make_float2(r.hi[2], r.lo[0]);
-  p[2] = make_float2(r.lo[1], r.lo[2]);
-}
 
 // Node records of an RVE solved by one CTA (shared or global memory), by
 // node id; also a cluster CTA's view of its own nodes, by local record.
+// Two arrays over the same n slots: (hi x, hi y, hi z, lo x) as one 16-byte
+// word, then (lo y, lo z) as one 8-byte word, so a record is one 128-bit
+// and one 64-bit access. A warp's gather of 32 scattered records then meets
+// fewer bank conflicts than with three 64-bit accesses to a 24-byte record
+// (a 128-bit access is served a quarter-warp at a time).
 struct LocalNodes {
-  float* hl;
-  __device__ __forceinline__ NodeRec load(int j) const { return load_rec(hl + 6 * j); }
-  __device__ __forceinline__ float* rec(int j) const { return hl + 6 * j; }
+  float4* a;
+  float2* b;
+  // the two arrays over n slots from p (16-byte aligned)
+  __device__ __forceinline__ static LocalNodes at(float* p, int64_t n) {
+    return {reinterpret_cast<float4*>(p), reinterpret_cast<float2*>(p + 4 * n)};
+  }
+  __device__ __forceinline__ NodeRec load(int j) const {
+    const float4 p = a[j];
+    const float2 q = b[j];
+    return {{p.x, p.y, p.z}, {p.w, q.x, q.y}};
+  }
+  __device__ __forceinline__ void put(int j, const NodeRec& r) const {
+    a[j] = make_float4(r.hi[0], r.hi[1], r.hi[2], r.lo[0]);
+    b[j] = make_float2(r.lo[1], r.lo[2]);
+  }
 };
 
 // Node records of an RVE split over the CTAs of a cluster, read through
 // distributed shared memory. CTA o owns a contiguous block of the free nodes
 // and one of the boundary nodes (both segments are Morton-sorted, so the two
 // blocks cover the same region of the RVE) and keeps their records at the
-// same shared-memory offset `base` in every CTA; an end node is given by its
-// code (owner << 24 | record).
+// same shared-memory offsets in every CTA (the two arrays of LocalNodes, at
+// base_a and base_b); an end node is given by its code (owner << 24 |
+// record).
 template <int CL>
 struct ClusterNodes {
-  uint32_t base;
+  uint32_t base_a, base_b;
+  __device__ __forceinline__ void point_at(const LocalNodes& own) {
+    base_a = static_cast<uint32_t>(__cvta_generic_to_shared(own.a));
+    base_b = static_cast<uint32_t>(__cvta_generic_to_shared(own.b));
+  }
   __device__ __forceinline__ NodeRec load(int code) const {
     const uint32_t o = static_cast<uint32_t>(code) >> 24;
-    const uint32_t a = cluster_addr(base + 24u * (static_cast<uint32_t>(code) & 0xFFFFFFu), o);
-    float2 p0, p1, p2;
-    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(p0.x), "=f"(p0.y) : "r"(a));
-    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(p1.x), "=f"(p1.y) : "r"(a + 8));
-    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(p2.x), "=f"(p2.y) : "r"(a + 16));
-    return {{p0.x, p0.y, p1.x}, {p1.y, p2.x, p2.y}};
+    const uint32_t j = static_cast<uint32_t>(code) & 0xFFFFFFu;
+    const uint32_t pa = cluster_addr(base_a + 16u * j, o);
+    const uint32_t pb = cluster_addr(base_b + 8u * j, o);
+    float4 p;
+    float2 q;
+    asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(p.x), "=f"(p.y), "=f"(p.z), "=f"(p.w)
+                 : "r"(pa));
+    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(q.x), "=f"(q.y) : "r"(pb));
+    return {{p.x, p.y, p.z}, {p.w, q.x, q.y}};
   }
 };
 
@@ -660,6 +674,10 @@ __device__ __forceinline__ void mixed_stress(const DevBatch& b, const RunArgs& a
   }
 }
 
+// Node slots rounded up to an even count, so that an array of records after
+// another starts on a 16-byte boundary.
+__host__ __device__ inline int64_t even_slots(int64_t n) { return (n + 1) & ~static_cast<int64_t>(1); }
+
 // Shared-memory floats per CTA of an RVE solved by CL CTAs: 9 per node slot
 // (displacement hi, lo and velocity; ceil(NF/CL) free plus ceil(NB/CL)
 // boundary slots), 15 with two copies of the node records, plus 4 per fiber
@@ -668,7 +686,7 @@ __device__ __forceinline__ void mixed_stress(const DevBatch& b, const RunArgs& a
 __host__ __device__ inline int64_t cluster_floats(int n_nodes, int n_free, int n_fibers, int cl,
                                                   bool all, bool two_copies = false) {
   const int64_t nb = n_nodes - n_free;
-  const int64_t cap = (static_cast<int64_t>(n_free) + cl - 1) / cl + (nb + cl - 1) / cl;
+  const int64_t cap = even_slots((static_cast<int64_t>(n_free) + cl - 1) / cl + (nb + cl - 1) / cl);
   const int64_t echunk = (static_cast<int64_t>(n_fibers) + cl - 1) / cl;
   return (two_copies ? 15 : 9) * cap + (all ? 4 * echunk : 0);
 }
@@ -710,7 +728,7 @@ __device__ __forceinline__ void mixed_prologue(const DevBatch& b, const MixedSta
       split(xn[k] - X[k], nr.hi[k], nr.lo[k]);
       vel[3 * li + k] = 0.f;
     }
-    store_rec(own.rec(li), nr);
+    own.put(li, nr);
     if (ramp && i >= NF) {
       // The boundary moves by d/n per step, d = (F - I) x0. The increment is
       // kept as an exact FP32 pair and accumulated without rounding into
@@ -739,7 +757,7 @@ __device__ __forceinline__ void ramp_boundary(const Rve& r, const LocalNodes& ow
   for (int i = g_lo + Group<NG>::tid(); i < g_hi; i += Group<NG>::kSize) {
     const float* rb = r.ramp + 12 * (i - NF);
     const int li = fchunk + (i - g_lo);
-    NodeRec nr = load_rec(own.rec(li));
+    NodeRec nr = own.load(li);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       float s, e;
@@ -747,7 +765,7 @@ __device__ __forceinline__ void ramp_boundary(const Rve& r, const LocalNodes& ow
       nr.hi[k] = s;
       nr.lo[k] = nr.lo[k] + (e + rb[3 + k]);
     }
-    store_rec((dst ? *dst : own).rec(li), nr);  // in place, or into the other copy
+    (dst ? *dst : own).put(li, nr);  // in place, or into the other copy
   }
 }
 
@@ -797,19 +815,19 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
   // velocities
   if (kAll || cluster_floats(N, NF, E, 1, true) <= smem_floats) {
     r.n = reinterpret_cast<float4*>(smem);
-    own.hl = smem + 4 * E;
+    own = LocalNodes::at(smem + 4 * E, N);
     vel = smem + 4 * E + 6 * N;
   } else if (cluster_floats(N, NF, E, 1, false) <= smem_floats) {
     r.n = ms.nrm + fo;
-    own.hl = smem;
+    own = LocalNodes::at(smem, N);
     vel = smem + 6 * N;
   } else if (6LL * N <= smem_floats) {
     r.n = ms.nrm + fo;
-    own.hl = smem;
+    own = LocalNodes::at(smem, N);
     vel = ms.v + 3 * no;
   } else {
     r.n = ms.nrm + fo;
-    own.hl = ms.u_hl + 6 * no;
+    own = {reinterpret_cast<float4*>(ms.u_hl) + no, reinterpret_cast<float2*>(ms.u_hl + 4 * nt) + no};
     vel = ms.v + 3 * no;
   }
   fv.p = r.n;
@@ -880,8 +898,7 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
         const float mc = cur.mm.y * c;
         const float km = hk * cur.mm.x;
         const int li = i - f_lo;
-        float* rec = own.rec(li);
-        NodeRec nr = load_rec(rec);
+        NodeRec nr = own.load(li);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
           float w = vel[3 * li + k];
@@ -889,7 +906,7 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
           vel[3 * li + k] = w;
           comp_add(nr.hi[k], nr.lo[k], h2 * w);
         }
-        store_rec(rec, nr);
+        own.put(li, nr);
         if (!more) break;
         cur = nxt;
         i = in;
@@ -916,7 +933,7 @@ __device__ void solve_rve_mixed(const DevBatch& b, const MixedState& ms, const R
     const int i = t < nfo ? f_lo + t : g_lo + (t - nfo);
     const int li = t < nfo ? t : fchunk + (t - nfo);
     const int64_t gi = kAll ? __ldg(ms.gnode + no + i) : no + i;  // batch node index
-    const NodeRec nr = load_rec(own.rec(li));
+    const NodeRec nr = own.load(li);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       const double Xk = b.X[k * nt + gi];
@@ -1049,7 +1066,7 @@ __device__ __forceinline__ double nodal_kick(const Law& L, const Nodes& u, const
       NodeRec nr = me;
 #pragma unroll
       for (int k = 0; k < 3; ++k) comp_add(nr.hi[k], nr.lo[k], h2 * wn[k]);
-      store_rec(nxt->rec(t), nr);
+      nxt->put(t, nr);
     }
     if (!more) break;
     t = tn;
@@ -1108,15 +1125,16 @@ __device__ void solve_rve_nodal(const DevBatch& b, const MixedState& ms, const R
   const int e_hi = min(E, e_lo + echunk);
   using Nodes = std::conditional_t<(CL > 1), ClusterNodes<CL>, LocalNodes>;
   Nodes u;         // every node of the RVE
-  LocalNodes own;  // the node records this CTA updates, by local index
-  own.hl = smem;
+  // the node records this CTA updates, by local index (an even slot count,
+  // so the next array starts on a 16-byte boundary)
+  const int64_t slots = even_slots(cap);
+  LocalNodes own = LocalNodes::at(smem, slots);
   // kDB: a second copy of the records, which each step drifts into; the two
   // copies swap roles every step
-  LocalNodes nxt;
-  nxt.hl = smem + 6 * cap;
-  float* vel = smem + (kDB ? 12 : 6) * cap;
+  LocalNodes nxt = LocalNodes::at(smem + 6 * slots, slots);
+  float* vel = smem + (kDB ? 12 : 6) * slots;
   if constexpr (CL > 1)
-    u.base = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+    u.point_at(own);
   else
     u = own;
   r.conn = ms.econn + fo;
@@ -1138,7 +1156,7 @@ __device__ void solve_rve_nodal(const DevBatch& b, const MixedState& ms, const R
     // boundary records in the second copy too (RAMP moves them into it every
     // step; RELAX never moves them); read there only after a step's barrier
     for (int t = tid; t < g_hi - g_lo; t += kThreadsMixed)
-      store_rec(nxt.rec(fchunk + t), load_rec(own.rec(fchunk + t)));
+      nxt.put(fchunk + t, own.load(fchunk + t));
   }
   double dt_crit = Ops::template combine<true>(
                        block_min<kThreadsMixed>(length_pass(r, u, e_lo, e_hi), red), cred) /
@@ -1187,14 +1205,13 @@ __device__ void solve_rve_nodal(const DevBatch& b, const MixedState& ms, const R
     if constexpr (!kDB) {
       // pass B: drift
       for (int t = tid; t < nfo; t += kThreadsMixed) {
-        float* rec = own.rec(t);
-        NodeRec nr = load_rec(rec);
+        NodeRec nr = own.load(t);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
           const float w = vel[3 * t + k];
           comp_add(nr.hi[k], nr.lo[k], h2 * w);
         }
-        store_rec(rec, nr);
+        own.put(t, nr);
       }
     }
     if (ramp) ramp_boundary(r, own, g_lo, g_hi, fchunk, kDB ? &nxt : nullptr);
@@ -1204,7 +1221,7 @@ __device__ void solve_rve_nodal(const DevBatch& b, const MixedState& ms, const R
       own = nxt;
       nxt = t;
       if constexpr (CL > 1)
-        u.base = static_cast<uint32_t>(__cvta_generic_to_shared(own.hl));
+        u.point_at(own);
       else
         u = own;
     }
